@@ -1,0 +1,380 @@
+#!/usr/bin/env python3
+"""Benchmark of the split-step Gross-Pitaevskii hot path on GB300.
+
+Workload (cfg1): 3D real-time GP, Strang splitting (NumModelSplit2), 256^3
+periodic box [0, 2pi]^3, V = 0, coeffD = -xi/sqrt(2), beta = 1/(sqrt(2) xi),
+xi = 0.05, psi0 = e^{i theta} with 64 seeded Fourier modes; dt = 2.5e-3.
+One bench step = one cfg1 run of 200 time steps through gpss_step (FP32 fused
+kernels, FP64 reductions), on a field resident in HBM.
+
+Metric: Mcell-steps/s = cells x time steps / seconds.  The field (134 MB FP32)
+is larger than L2 and every pass streams 268 MB, so no L2 flush is needed.
+
+JSON line keys beyond the base contract:
+  e2e            same metric through the public API with host buffers: every
+                 step uploads psi (FP64, pinned), runs the 200 steps and
+                 downloads psi.
+  roofline       the dominant kernel (fused directional pass) against the
+                 measured HBM copy bandwidth; algorithmic bytes = 16 B/cell/pass.
+  cpu_baseline   the CPU oracle (FP64 C restatement, OpenMP) on a bounded
+                 sample of the same workload.
+  fp64_plain     the FP64 plain kernels (reference stage order) on the same
+                 workload, the comparison the headline metric names.
+
+--impl reference times the CPU restatement of the reference path (the
+reference itself is Julia + FFTW, which does not exist on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CELLS_N = 256
+TIMESTEPS_PER_STEP = 200
+BYTES_PER_CELL_PASS = 16  # FP32 complex read + write
+PASSES_PER_TIMESTEP = 3   # merged Strang: 3 passes per step (+3 for the final half step)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpss", choices=["gpss", "reference"])
+    ap.add_argument("--n", type=int, default=CELLS_N, help="grid points per axis (default 256)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for torchrun launches (gloo: host-side only)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.out = ""
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            self.out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_tag):
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+# ----------------------------------------------------------------- CPU arm --
+def oracle_mod():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gp_oracle
+    gp_oracle.build()
+    return gp_oracle
+
+
+def cpu_sample(c, O, timesteps=1, nthreads=0):
+    """One bounded sample of the workload on the CPU oracle; returns (cell-steps/s, cores)."""
+    cores = nthreads or os.cpu_count() or 1
+    psi = c["psi"]
+    t0 = time.perf_counter()
+    O.c_step(psi, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"], nsteps=timesteps,
+             dt=c["dt"], nthreads=cores)
+    dt = time.perf_counter() - t0
+    cells = float(math.prod(c["shape"]))
+    return cells * timesteps / dt, cores, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import importlib
+    import __graft_entry__ as g
+    g.load_package()
+    W = importlib.import_module("sfd_gb300.workloads")
+    c = W.cfg1(args.n)
+    O = oracle_mod()
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(c, O, 1, cores)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, _, dt = cpu_sample(c, O, 1, cores)
+        vals.append(v)
+        secs += dt
+    value = (float(math.prod(c["shape"])) * args.steps) / secs / 1e6
+    sample = f"1 Strang time step of cfg1 at {args.n}^3 per bench step (FP64, own radix-2 FFT, OpenMP)"
+    line = {
+        "impl": "reference", "metric": "GP split-step Mcell-steps/s at 256^3", "value": value,
+        "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cfg1 phase field)",
+        "config": {"workload": f"cfg1: 3D GP Strang {args.n}^3, V=0, dt=2.5e-3", "grid": [args.n] * 3,
+                   "timesteps_per_step": 1},
+        "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of NumModelSplit2 (oracle/gp_oracle.c); the reference's Julia/FFTW "
+                "runtime is not installed on this machine",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- GPU arm --
+def run_gpss(args, rank, world, local):
+    import importlib
+    import numpy as np
+    import __graft_entry__ as g
+    sfd = g.load_package()
+    from sfd_gb300 import _lib
+    W = importlib.import_module("sfd_gb300.workloads")
+    L = _lib.lib()
+    dist = Dist(world)
+    _lib.check(L.gpss_select_device(local))
+    c = W.cfg1(args.n)
+    cells = float(math.prod(c["shape"]))
+    nt = TIMESTEPS_PER_STEP
+
+    grid = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(grid)
+    f.phi = c["psi"]
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+    model = sfd.NumModelSplit2(f, p, c["dt"], nt, nt, precision="fp32")
+    h = model.handle
+    ck = lambda rc: _lib.check(rc, h)
+
+    # ---- device-resident throughput (value)
+    for _ in range(args.warmup):
+        ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+    ck(L.gpss_sync(h))
+    dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = L.gpss_launch_count(h)
+    ck(L.gpss_event_record(h, 0))
+    for _ in range(args.steps):
+        ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+    ck(L.gpss_event_record(h, 1))
+    ms = ctypes.c_float()
+    ck(L.gpss_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+    launches = L.gpss_launch_count(h) - l0
+    clk = clocks.stop()
+    dist.barrier()
+    t_ms = dist.max(ms.value)
+    value = world * cells * nt * args.steps / (t_ms / 1e3) / 1e6
+
+    # ---- dominant kernel timing (roofline): each fused pass alone, CUDA events
+    per_axis = {}
+    for axis in range(3):
+        out = ctypes.c_double()
+        ck(L.gpss_time_pass(h, axis, 1 if axis == 2 else 0, 20, c["dt"], ctypes.byref(out)))
+        per_axis["xyz"[axis]] = out.value
+    dom = max(per_axis, key=per_axis.get)
+    dom_ms = per_axis[dom]
+    alg_bytes = BYTES_PER_CELL_PASS * cells
+    peak, peak_kind = measured_hbm_peak()
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
+    tag = f"pass_fp32_{dom}_cfg1_{args.n}"
+    traffic = profiled_traffic(tag)
+    # whole-step bandwidth: 3 passes per merged step plus the final half step per call
+    passes_per_call = PASSES_PER_TIMESTEP * (nt + 1)
+    step_gbs = BYTES_PER_CELL_PASS * cells * passes_per_call * args.steps / (t_ms / 1e3) / 1e9
+
+    # ---- end to end through the public API with host buffers
+    nbytes = int(cells) * 16
+    hbuf = ctypes.c_void_p()
+    _lib.check(L.gpss_host_alloc(ctypes.byref(hbuf), nbytes))
+    host = np.frombuffer((ctypes.c_char * nbytes).from_address(hbuf.value), dtype=np.complex128)
+    host[:] = c["psi"].reshape(-1, order="F")
+    hp = ctypes.cast(hbuf, ctypes.POINTER(ctypes.c_double))
+    e2e_steps = max(3, min(args.steps, 10))
+    ck(L.gpss_upload(h, hp))
+    ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+    ck(L.gpss_download(h, hp))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ck(L.gpss_upload(h, hp))
+        ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+        ck(L.gpss_download(h, hp))
+    ck(L.gpss_sync(h))
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = world * cells * nt * e2e_steps / e2e_s / 1e6
+    _lib.check(L.gpss_host_free(hbuf))
+    model.close(download=False)
+
+    # ---- FP64 plain kernels on the same workload (fewer time steps)
+    fp64 = None
+    if not args.no_fp64:
+        f64 = sfd.Field(grid)
+        f64.phi = c["psi"]
+        p64 = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f64), coeffD=c["coeffD"], beta=c["beta"])
+        m64 = sfd.NumModelSplit2(f64, p64, c["dt"], 10, 10, precision="fp64", form="plain")
+        h64 = m64.handle
+        k64 = 10
+        _lib.check(L.gpss_step(h64, 2, 2, 0, c["dt"], None), h64)
+        _lib.check(L.gpss_event_record(h64, 0), h64)
+        _lib.check(L.gpss_step(h64, k64, 2, 0, c["dt"], None), h64)
+        _lib.check(L.gpss_event_record(h64, 1), h64)
+        ms64 = ctypes.c_float()
+        _lib.check(L.gpss_event_elapsed(h64, 0, 1, ctypes.byref(ms64)), h64)
+        m64.close(download=False)
+        v64 = cells * k64 / (ms64.value / 1e3) / 1e6
+        fp64 = {"value": v64, "unit": "Mcell-steps/s", "timesteps": k64,
+                "ms_per_timestep": ms64.value / k64, "fp32_fused_over_fp64_plain": value / world / v64}
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        O = oracle_mod()
+        v, cores, dt = cpu_sample(c, O, 1, os.cpu_count() or 1)
+        steps = max(1, min(8, int(15.0 / max(dt, 1e-3))))
+        if steps > 1:
+            v, cores, dt = cpu_sample(c, O, steps, os.cpu_count() or 1)
+        cpu = {"value": v / 1e6, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{steps} Strang time step(s) of cfg1 at {args.n}^3 on the FP64 C oracle "
+                         f"(own radix-2 FFT, OpenMP), {dt:.1f} s"}
+
+    dist.close()
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "GP split-step Mcell-steps/s at 256^3: FP32 fused vs FP64 plain @ relL2<=1e-5",
+        "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded cfg1 phase field, 64 modes |k|<=4)",
+        "config": {"workload": f"cfg1: 3D real-time GP Strang (NumModelSplit2), {args.n}^3 on [0,2pi]^3, "
+                               "V=0, xi=0.05, c=1, dt=2.5e-3, FP32 fused kernels",
+                   "grid": [args.n] * 3, "timesteps_per_step": nt,
+                   "l2": "inputs larger than L2 (134 MB field, 268 MB streamed per pass); no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e, "unit": "Mcell-steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": f"fused {dom} pass",
+                     "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                     else "fallback 6800 GB/s",
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "ms_per_launch": per_axis,
+                     "whole_step_gbs": step_gbs},
+        "cpu_baseline": cpu,
+        "fp64_plain": fp64,
+    }
+    if clk:
+        line["clocks"] = clk
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gpss(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,169 @@
+/*
+ * gpss.h -- C ABI of libgpss.so, the GB300 split-step Gross-Pitaevskii
+ * library.  It replaces the time-stepping hot path of SuperfluidDynamics.jl
+ * (NumModelSplit1 / NumModelSplit2 on a periodic Grid) behind plain C types so
+ * that Julia can bind it with ccall.
+ *
+ * Conventions
+ *   - Fields are column-major with x fastest and complex values interleaved
+ *     (re, im) as doubles: the memory of a Julia Array{ComplexF64} (the parent
+ *     of Field.ϕ, src/Discretization/Fields.jl:94-157).  Potentials are real
+ *     doubles of the same shape (param.pot.V, src/Potentials/quadratic.jl:61-67).
+ *   - Every entry returns 0 (GPSS_OK) or a negative GPSS_E* code; the message
+ *     is available from gpss_last_error().  No entry traps or aborts.
+ *   - A context owns all of its device memory and one CUDA stream; it is not
+ *     thread-safe.  Distinct contexts may be used from distinct threads.
+ *   - Host pointers are only read or written during the call; none is kept.
+ */
+#ifndef GPSS_H
+#define GPSS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPSS_OK 0
+#define GPSS_EINVAL (-1)      /* bad argument: sizes, null pointers, ... */
+#define GPSS_ENOMEM (-2)      /* device or host allocation failed */
+#define GPSS_ECUDA (-3)       /* a CUDA runtime call failed */
+#define GPSS_ENONFINITE (-4)  /* a reduction saw NaN/Inf in the field */
+#define GPSS_ETIMEOUT (-5)    /* a bounded device-side wait gave up */
+#define GPSS_ESTATE (-6)      /* call out of order (e.g. no field uploaded) */
+
+/* precision of the device field and of the FFT/phase arithmetic */
+#define GPSS_FP64 64
+#define GPSS_FP32 32
+
+/* gpss_create flags */
+#define GPSS_FLAG_PLAIN 1     /* reference stage order: FFT, multiply, iFFT, NL as
+                                 separate launches (no fusion, no merging) */
+#define GPSS_FLAG_NOMERGE 2   /* fused passes, but never merge the trailing and
+                                 leading half kinetic steps of consecutive steps */
+
+/* split schemes of gpss_step */
+#define GPSS_LIE 1            /* NumModelSplit1: L(dt) N(dt) */
+#define GPSS_STRANG 2         /* NumModelSplit2: L(dt/2) N(dt) L(dt/2) */
+
+typedef struct gpss_ctx gpss_ctx;
+
+/* Diagnostics of the field at the end of a gpss_step call (FP64). */
+typedef struct gpss_diag {
+    double mass;        /* sum |psi|^2 dV  (= norm(f)^2, Fields.jl:172-180) */
+    double energy[5];   /* E_Omega, E_Delta, E_beta, E, mu (GrossPitaevskii.jl:61-136) */
+    int64_t steps;      /* steps performed by the call */
+} gpss_diag;
+
+/* Library version string. */
+const char *gpss_version(void);
+
+/*
+ * Create a context for an ndim-dimensional periodic grid of n[0] x n[1]
+ * [x n[2]] nodes on [lo[a], hi[a]).  Replaces Grid(size, bounds)
+ * (src/Discretization/Grids.jl:64-129) + Field(grid, ComplexField())
+ * (src/Discretization/Fields.jl:94-157) + Plan(f) (src/Discretization/Plans.jl:821-854,
+ * 958-999).  ndim is 2 or 3; each n[a] is a power of two in [2, 256].
+ * precision is GPSS_FP64 or GPSS_FP32; flags is a GPSS_FLAG_* mask.
+ */
+int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, const double *hi,
+                int precision, int flags);
+
+/* Release every device resource of the context (NULL is accepted). */
+void gpss_destroy(gpss_ctx *ctx);
+
+/* Last error message of ctx (or of the last failed gpss_create when ctx is NULL). */
+const char *gpss_last_error(const gpss_ctx *ctx);
+
+/*
+ * Equation parameters: i dpsi/dt = coeffD Lap psi + beta |psi|^2 psi + V psi - i Omega Lz psi.
+ * Replaces GrossPitaevskiiParameters(coeffΔ, β, pot, Ω) (src/Parameters/Parameters.jl:17-55).
+ */
+int gpss_set_params(gpss_ctx *ctx, double coeffD, double beta, double omega);
+
+/* Potential V (real, field shape).  NULL selects PotentialZero
+ * (src/Potentials/Potentials.jl:12-25); otherwise param.pot.V. */
+int gpss_set_potential(gpss_ctx *ctx, const double *V);
+
+/* Copy psi (interleaved complex doubles) to / from the device field. */
+int gpss_upload(gpss_ctx *ctx, const double *psi);
+int gpss_download(gpss_ctx *ctx, double *psi);
+
+/*
+ * nsteps split steps of size dt.  scheme: GPSS_STRANG replaces
+ * timeStep!(::NumModelSplit2) (src/NumModels/GrossPitaevskii/splitting.jl:149-154),
+ * GPSS_LIE replaces timeStep!(::NumModelSplit1) (splitting.jl:78-82).
+ * imag != 0 integrates in imaginary time and renormalises the field to unit
+ * mass after every step (an extension; the reference has no imaginary-time
+ * split step).  diag may be NULL; when given, it receives the mass and
+ * energies of the final field.
+ */
+int gpss_step(gpss_ctx *ctx, int nsteps, int scheme, int imag, double dt, gpss_diag *diag);
+
+/*
+ * Energies of the current field: out = {E_Omega, E_Delta, E_beta, E, mu}.
+ * Replaces energy(n) (src/NumModels/GrossPitaevskii/GrossPitaevskii.jl:61-92 2D,
+ * 106-136 3D; the 3D method prints no mu, the 2D formula is used for it).
+ */
+int gpss_energy(gpss_ctx *ctx, double *out);
+
+/* sum |psi|^2 dV of the current field (norm(f)^2, src/Discretization/Fields.jl:172-180). */
+int gpss_mass(gpss_ctx *ctx, double *out);
+
+/* norm(f) (Fields.jl:172-180) and normalize! (Fields.jl:196-200) on the device field. */
+int gpss_norm(gpss_ctx *ctx, double *out);
+int gpss_normalize(gpss_ctx *ctx);
+
+/*
+ * Imaginary-time ground state: Strang steps of dt with unit-mass
+ * renormalisation until |mu_k - mu_{k-1}| < tol, mu being evaluated every
+ * check_every steps, or max_steps steps.  An extension (the reference reaches
+ * ground states with Backward-Euler / Crank-Nicolson,
+ * src/NumModels/GrossPitaevskii/backward-euler.jl:72-85).
+ */
+int gpss_ground_state(gpss_ctx *ctx, double dt, double tol, int64_t max_steps, int check_every,
+                      double *mu_out, int64_t *steps_out);
+
+/* ---- timing and integration helpers (no reference counterpart) ---- */
+
+/* Make `device` the CUDA device that later gpss_create calls on this host
+ * thread use (the library links its own CUDA runtime, whose current device
+ * is separate from any other runtime loaded in the process). */
+int gpss_select_device(int device);
+
+/* Number of CUDA devices visible to the library (0 when there is none). */
+int gpss_device_count(void);
+
+/* Block the host until the context's stream is idle. */
+int gpss_sync(gpss_ctx *ctx);
+
+/* Record CUDA event `slot` (0..7) on the context's stream. */
+int gpss_event_record(gpss_ctx *ctx, int slot);
+
+/* Milliseconds between two recorded events (synchronises on `b`). */
+int gpss_event_elapsed(gpss_ctx *ctx, int a, int b, float *ms);
+
+/* Number of kernel launches issued by the context since creation. */
+int64_t gpss_launch_count(const gpss_ctx *ctx);
+
+/*
+ * Time each directional pass kernel of one fused kinetic step in isolation:
+ * runs `reps` launches of the pass along `axis` (0 = x, 1 = y, 2 = z; mode 0 =
+ * fused kinetic pass, 1 = fused kinetic pass with the nonlinear epilogue) on
+ * the current field, bracketed by CUDA events, and returns the mean
+ * milliseconds per launch.  The field is advanced by those launches.
+ */
+int gpss_time_pass(gpss_ctx *ctx, int axis, int mode, int reps, double dt, double *ms_per_launch);
+
+/* Page-locked host buffer helpers for fast uploads/downloads. */
+int gpss_host_alloc(void **ptr, int64_t bytes);
+int gpss_host_free(void *ptr);
+
+/* Device memory held by the context, in bytes. */
+int64_t gpss_device_bytes(const gpss_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPSS_H */

@@ -1,0 +1,579 @@
+/*
+ * gp_oracle.c -- CPU restatement (FP64) of SuperfluidDynamics.jl's split-step
+ * Gross-Pitaevskii path, used as the CHECKER of the CUDA library.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference arm of bench.py load this file's library.  The
+ * product path (libgpss.so) never links, loads or calls it.
+ *
+ * What it restates (file:line in the reference project):
+ *   grid nodes      src/Discretization/Grids.jl:78-84   x = LinRange(lo,hi,n+1)[1:end-1]
+ *   wavenumbers     src/Discretization/Plans.jl:829-830, 967-969   fftfreq(n, 2pi/dx)
+ *   Strang step     src/NumModels/GrossPitaevskii/splitting.jl:149-154
+ *   Lie step        src/NumModels/GrossPitaevskii/splitting.jl:78-82
+ *   kinetic flow    src/NumModels/GrossPitaevskii/splitting.jl:156-203
+ *   nonlinear flow  src/NumModels/GrossPitaevskii/splitting.jl:205-209
+ *   FFT / iFFT      src/Discretization/Plans.jl:1132-1250 (forward unnormalised,
+ *                   inverse = backward transform then *1/n, as AbstractFFTs' ldiv!)
+ *   norm            src/Discretization/Fields.jl:172-180
+ *   energy          src/NumModels/GrossPitaevskii/GrossPitaevskii.jl:61-136 with
+ *                   computeDerivatives!(GradientRotField) src/NumModels/derivatives.jl:27-56, 90-126
+ *   imaginary time  extension (no split-step counterpart in the reference): the
+ *                   same stages with t -> -i tau and a unit-mass renormalisation
+ *                   (normalize!, Fields.jl:196-200) after every step.
+ *
+ * The FFT here is this file's own iterative radix-2 transform (FFTW, which the
+ * reference calls, is not available); results therefore agree with the
+ * reference at the round-off level, and parity is pinned by the reference's
+ * analytic known-answer tests (test/runtests.jl:29-90, 644-671, 718-725).
+ *
+ * Layout: column-major, x fastest (Julia Array order), complex interleaved
+ * (re, im) doubles, exactly the memory of a Julia Array{ComplexF64}.
+ *
+ * Compiled with -ffp-contract=off so x86 and Arm hosts round identically.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OR_TWO_PI 6.283185307179586 /* Float64(2pi), as Julia's 2pi literal */
+
+typedef struct { double re, im; } ocplx;
+
+/* ---------------------------------------------------------------- grid --- */
+
+/* Julia Base.lerpi: t = j/d; (1-t)*a + t*b  (base/range.jl) */
+static double lerpi(int64_t j, int64_t d, double a, double b)
+{
+    double t = (double)j / (double)d;
+    return (1.0 - t) * a + t * b;
+}
+
+/* Grids.jl:78-84: x = LinRange(lo, hi, n+1)[1:end-1].  Indexing a LinRange
+ * with a range builds LinRange(x[1], x[n], n), whose entries are lerps between
+ * those two end points. */
+void or_grid_coords(int64_t n, double lo, double hi, double *x)
+{
+    if (n <= 1) { x[0] = lo; return; }
+    double first = lerpi(0, n, lo, hi);
+    double last = lerpi(n - 1, n, lo, hi);
+    for (int64_t i = 0; i < n; i++) x[i] = lerpi(i, n - 1, first, last);
+}
+
+/* Plans.jl:829-830: xi = fftfreq(n, 2pi/dx) (AbstractFFTs.Frequencies:
+ * entry i is (i-1 - (i <= (n+1)>>1 ? 0 : n)) * (fs/n)). */
+void or_fftfreq(int64_t n, double dx, double *xi)
+{
+    double fs = OR_TWO_PI / dx;
+    double mult = fs / (double)n;
+    int64_t nneg = (n + 1) >> 1;
+    for (int64_t i = 0; i < n; i++) {
+        int64_t k = (i < nneg) ? i : i - n;
+        xi[i] = (double)k * mult;
+    }
+}
+
+/* ----------------------------------------------------------------- FFT --- */
+
+/* (cos, sin) of 2 pi k / n, reduced to the first octant for accuracy and
+ * exact symmetries. */
+static void unit_root(int64_t k, int64_t n, double *c, double *s)
+{
+    k %= n; if (k < 0) k += n;
+    /* quadrant */
+    int64_t q = (4 * k) / n;          /* 0..3 */
+    int64_t r4 = 4 * k - q * n;       /* remainder in units of 1/(4n) turns, [0,n) */
+    double cc, ss;
+    if (2 * r4 <= n) {
+        double a = 0.5 * M_PI * (double)r4 / (double)n;
+        cc = cos(a); ss = sin(a);
+    } else {
+        double a = 0.5 * M_PI * (double)(n - r4) / (double)n;
+        cc = sin(a); ss = cos(a);
+    }
+    switch (q) {
+    case 0: *c = cc;  *s = ss;  break;
+    case 1: *c = -ss; *s = cc;  break;
+    case 2: *c = -cc; *s = -ss; break;
+    default:*c = ss;  *s = -cc; break;
+    }
+}
+
+typedef struct {
+    int64_t n;
+    int pow2;
+    ocplx *tw;       /* exp(-2 pi i k / n), k < n */
+} fftplan;
+
+static int is_pow2(int64_t n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static int plan_make(fftplan *p, int64_t n)
+{
+    p->n = n;
+    p->pow2 = is_pow2(n);
+    p->tw = (ocplx *)malloc(sizeof(ocplx) * (size_t)(n > 0 ? n : 1));
+    if (!p->tw) return -1;
+    for (int64_t k = 0; k < n; k++) {
+        double c, s;
+        unit_root(k, n, &c, &s);
+        p->tw[k].re = c;
+        p->tw[k].im = -s;
+    }
+    return 0;
+}
+
+static void plan_free(fftplan *p) { free(p->tw); p->tw = NULL; }
+
+/* Unnormalised DFT of one contiguous line.  sign = -1 forward (FFTW_FORWARD,
+ * exp(-2 pi i jk/n)), +1 backward.  tmp holds n entries of scratch. */
+static void fft_line(const fftplan *p, ocplx *a, ocplx *tmp, int sign)
+{
+    int64_t n = p->n;
+    if (n == 1) return;
+    if (!p->pow2) { /* direct O(n^2) DFT for sizes that are not powers of two */
+        for (int64_t k = 0; k < n; k++) {
+            double sr = 0.0, si = 0.0;
+            for (int64_t j = 0; j < n; j++) {
+                int64_t m = (j * k) % n;
+                double wr = p->tw[m].re, wi = sign < 0 ? p->tw[m].im : -p->tw[m].im;
+                sr += a[j].re * wr - a[j].im * wi;
+                si += a[j].re * wi + a[j].im * wr;
+            }
+            tmp[k].re = sr; tmp[k].im = si;
+        }
+        memcpy(a, tmp, sizeof(ocplx) * (size_t)n);
+        return;
+    }
+    /* bit reversal permutation */
+    int64_t j = 0;
+    for (int64_t i = 0; i < n - 1; i++) {
+        if (i < j) { ocplx t = a[i]; a[i] = a[j]; a[j] = t; }
+        int64_t m = n >> 1;
+        while (m >= 1 && j >= m) { j -= m; m >>= 1; }
+        j += m;
+    }
+    /* iterative radix-2 decimation in time */
+    for (int64_t len = 2; len <= n; len <<= 1) {
+        int64_t half = len >> 1, step = n / len;
+        for (int64_t i = 0; i < n; i += len) {
+            for (int64_t k = 0; k < half; k++) {
+                double wr = p->tw[k * step].re;
+                double wi = sign < 0 ? p->tw[k * step].im : -p->tw[k * step].im;
+                ocplx u = a[i + k], v = a[i + k + half];
+                double tr = v.re * wr - v.im * wi;
+                double ti = v.re * wi + v.im * wr;
+                a[i + k].re = u.re + tr; a[i + k].im = u.im + ti;
+                a[i + k + half].re = u.re - tr; a[i + k + half].im = u.im - ti;
+            }
+        }
+    }
+    (void)tmp;
+}
+
+/* ---------------------------------------------------------- geometry ----- */
+
+typedef struct {
+    int ndim;
+    int64_t n[3];
+    double lo[3], hi[3], L[3], d[3];
+    int64_t total;
+    double *coord[3];
+    double *xi[3];
+    fftplan plan[3];
+} ogrid;
+
+static void grid_free(ogrid *g)
+{
+    for (int a = 0; a < 3; a++) {
+        free(g->coord[a]); free(g->xi[a]);
+        if (a < g->ndim) plan_free(&g->plan[a]);
+        g->coord[a] = g->xi[a] = NULL;
+    }
+}
+
+static int grid_make(ogrid *g, int ndim, const int64_t *n, const double *lo, const double *hi)
+{
+    memset(g, 0, sizeof(*g));
+    if (ndim < 1 || ndim > 3) return -1;
+    g->ndim = ndim;
+    g->total = 1;
+    for (int a = 0; a < 3; a++) {
+        g->n[a] = a < ndim ? n[a] : 1;
+        if (g->n[a] <= 0) return -1;
+        g->lo[a] = a < ndim ? lo[a] : 0.0;
+        g->hi[a] = a < ndim ? hi[a] : 1.0;
+        g->L[a] = g->hi[a] - g->lo[a];
+        g->d[a] = g->L[a] / (double)g->n[a];          /* Grids.jl:80 */
+        g->total *= g->n[a];
+        g->coord[a] = (double *)malloc(sizeof(double) * (size_t)g->n[a]);
+        g->xi[a] = (double *)malloc(sizeof(double) * (size_t)g->n[a]);
+        if (!g->coord[a] || !g->xi[a]) { grid_free(g); return -1; }
+        or_grid_coords(g->n[a], g->lo[a], g->hi[a], g->coord[a]);
+        or_fftfreq(g->n[a], g->d[a], g->xi[a]);
+        if (a < ndim && plan_make(&g->plan[a], g->n[a])) { grid_free(g); return -1; }
+    }
+    return 0;
+}
+
+static double cell_volume(const ogrid *g)
+{
+    double v = 1.0;
+    for (int a = 0; a < g->ndim; a++) v *= g->d[a];
+    return v;
+}
+
+/* x * dx * dy [* dz], left to right as Julia evaluates `s * Δx * Δy * Δz` */
+static double times_cell(const ogrid *g, double x)
+{
+    for (int a = 0; a < g->ndim; a++) x *= g->d[a];
+    return x;
+}
+
+/* Julia's sum is pairwise; so is this one (block of 1024 leaves). */
+static double pairwise_sum(const double *v, int64_t n)
+{
+    if (n <= 1024) {
+        double s = 0.0;
+        for (int64_t i = 0; i < n; i++) s += v[i];
+        return s;
+    }
+    int64_t h = n / 2;
+    return pairwise_sum(v, h) + pairwise_sum(v + h, n - h);
+}
+
+/* --------------------------------------------------- directional passes -- */
+
+/* For each line along `axis`: FFT, multiply by a per-(line, k) factor, iFFT.
+ * mode selects the factor (all of splitting.jl:167/172/190/195/200):
+ *   real time   exp(i (cD xi^2 - Om y xi) dtl)   (x)
+ *               exp(i (cD xi^2 + Om x xi) dtl)   (y)
+ *               exp(i  cD xi^2 dtl)              (z)
+ *   imag time   the same with t -> -i tau: exp((cD xi^2 -/+ Om c xi) dtl).
+ */
+static void kinetic_axis(const ogrid *g, ocplx *psi, int axis, double cD, double Om,
+                         double dtl, int imag)
+{
+    int64_t n = g->n[axis];
+    int64_t nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : nx * ny);
+    int64_t nlines = g->total / n;
+    const double *xi = g->xi[axis];
+    double inv_n = 1.0 / (double)n;
+    (void)nz;
+#pragma omp parallel
+    {
+        ocplx *line = (ocplx *)malloc(sizeof(ocplx) * (size_t)n);
+        ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)n);
+#pragma omp for schedule(static)
+        for (int64_t l = 0; l < nlines; l++) {
+            int64_t base, other;
+            if (axis == 0) {          /* lines indexed by (j, k) */
+                base = l * nx;
+                other = l % ny;       /* y index */
+            } else if (axis == 1) {   /* lines indexed by (i, k) */
+                int64_t i = l % nx, k = l / nx;
+                base = i + k * nx * ny;
+                other = i;            /* x index */
+            } else {
+                base = l;
+                other = 0;
+            }
+            for (int64_t p = 0; p < n; p++) line[p] = psi[base + p * stride];
+            fft_line(&g->plan[axis], line, tmp, -1);
+            /* coordinate of this line that enters the rotation term */
+            double c = 0.0;
+            if (axis == 0 && g->ndim >= 2) c = g->coord[1][other];
+            else if (axis == 1) c = g->coord[0][other];
+            for (int64_t k = 0; k < n; k++) {
+                double xk = xi[k], ph;
+                /* Julia: coeffD * xi^2 -/+ Om * c * xi  (xi^2 == xi*xi) */
+                if (axis == 0) ph = cD * (xk * xk) - Om * c * xk;
+                else if (axis == 1) ph = cD * (xk * xk) + Om * c * xk;
+                else ph = cD * (xk * xk);
+                double fr, fi;
+                if (!imag) { double t = ph * dtl; fr = cos(t); fi = sin(t); }
+                else { fr = exp(ph * dtl); fi = 0.0; }
+                double ar = line[k].re, ai = line[k].im;
+                line[k].re = fr * ar - fi * ai;
+                line[k].im = fr * ai + fi * ar;
+            }
+            fft_line(&g->plan[axis], line, tmp, +1);
+            for (int64_t p = 0; p < n; p++) {
+                psi[base + p * stride].re = line[p].re * inv_n;
+                psi[base + p * stride].im = line[p].im * inv_n;
+            }
+        }
+        free(line); free(tmp);
+    }
+}
+
+/* splitting.jl:156-203 solveLapRot!: x, then y, then z. */
+static void solve_lap_rot(const ogrid *g, ocplx *psi, double cD, double Om, double dtl, int imag)
+{
+    for (int a = 0; a < g->ndim; a++) kinetic_axis(g, psi, a, cD, Om, dtl, imag);
+}
+
+/* splitting.jl:205-209 solveNL!: psi <- exp(-i (V + beta |psi|^2) dtl) psi;
+ * imaginary time: psi <- exp(-(V + beta |psi|^2) dtl) psi. */
+static void solve_nl(const ogrid *g, ocplx *psi, const double *V, double beta, double dtl, int imag)
+{
+    int64_t N = g->total;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        double ar = psi[i].re, ai = psi[i].im;
+        double rho = ar * ar + ai * ai;                 /* abs2 */
+        double r = (V ? V[i] : 0.0) + beta * rho;
+        double fr, fi;
+        if (!imag) { double t = -r * dtl; fr = cos(t); fi = sin(t); }
+        else { fr = exp(-r * dtl); fi = 0.0; }
+        psi[i].re = fr * ar - fi * ai;
+        psi[i].im = fr * ai + fi * ar;
+    }
+}
+
+static double sum_abs2(const ogrid *g, const ocplx *psi)
+{
+    int64_t N = g->total;
+    double *tmp = (double *)malloc(sizeof(double) * (size_t)N);
+    if (!tmp) return NAN;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) tmp[i] = psi[i].re * psi[i].re + psi[i].im * psi[i].im;
+    double s = pairwise_sum(tmp, N);
+    free(tmp);
+    return s;
+}
+
+/* Fields.jl:172-180 */
+static double field_norm(const ogrid *g, const ocplx *psi)
+{
+    return sqrt(sum_abs2(g, psi)) * sqrt(cell_volume(g));
+}
+
+/* ------------------------------------------------------------ public API -- */
+
+double or_norm(int ndim, const int64_t *n, const double *lo, const double *hi, const double *psi)
+{
+    ogrid g;
+    if (grid_make(&g, ndim, n, lo, hi)) return NAN;
+    double r = field_norm(&g, (const ocplx *)psi);
+    grid_free(&g);
+    return r;
+}
+
+/* Batched 1D FFT along one axis (unnormalised forward, or backward*1/n when
+ * inverse != 0) -- Plans.jl mul_x!/ldiv_x! etc. without the pencil moves. */
+int or_fft_axis(int ndim, const int64_t *n, double *psi, int axis, int inverse)
+{
+    ogrid g;
+    const double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    if (axis < 0 || axis >= ndim) { grid_free(&g); return -1; }
+    int64_t len = g.n[axis], nx = g.n[0], ny = g.n[1];
+    int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : nx * ny);
+    int64_t nlines = g.total / len;
+    ocplx *p = (ocplx *)psi;
+    ocplx *line = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+    ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+    for (int64_t l = 0; l < nlines; l++) {
+        int64_t base = axis == 0 ? l * nx : (axis == 1 ? (l % nx) + (l / nx) * nx * ny : l);
+        for (int64_t q = 0; q < len; q++) line[q] = p[base + q * stride];
+        fft_line(&g.plan[axis], line, tmp, inverse ? +1 : -1);
+        double s = inverse ? 1.0 / (double)len : 1.0;
+        for (int64_t q = 0; q < len; q++) {
+            p[base + q * stride].re = line[q].re * s;
+            p[base + q * stride].im = line[q].im * s;
+        }
+    }
+    free(line); free(tmp);
+    grid_free(&g);
+    return 0;
+}
+
+/*
+ * nsteps split steps.  scheme 2 = Strang (NumModelSplit2.timeStep!,
+ * splitting.jl:149-154), scheme 1 = Lie (NumModelSplit1.timeStep!, :78-82).
+ * imag != 0: imaginary time with unit-mass renormalisation after each step.
+ * V may be NULL (PotentialZero).  nthreads <= 0 keeps the OpenMP default.
+ */
+int or_step(int ndim, const int64_t *n, const double *lo, const double *hi,
+            double cD, double beta, double Om, const double *V, double *psi,
+            int nsteps, int scheme, int imag, double dt, int nthreads)
+{
+    ogrid g;
+    if (scheme != 1 && scheme != 2) return -1;
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+#ifdef _OPENMP
+    int saved = omp_get_max_threads();
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    ocplx *p = (ocplx *)psi;
+    for (int s = 0; s < nsteps; s++) {
+        if (scheme == 2) {
+            solve_lap_rot(&g, p, cD, Om, dt * 0.5, imag);
+            solve_nl(&g, p, V, beta, dt, imag);
+            solve_lap_rot(&g, p, cD, Om, dt * 0.5, imag);
+        } else {
+            solve_lap_rot(&g, p, cD, Om, dt, imag);
+            solve_nl(&g, p, V, beta, dt, imag);
+        }
+        if (imag) {                       /* normalize!, Fields.jl:196-200 */
+            double nrm = field_norm(&g, p);
+            int64_t N = g.total;
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < N; i++) { p[i].re /= nrm; p[i].im /= nrm; }
+        }
+    }
+#ifdef _OPENMP
+    omp_set_num_threads(saved);
+#endif
+    grid_free(&g);
+    return 0;
+}
+
+/*
+ * Spectral derivatives of GradientRotField (derivatives.jl:27-56 for 2D,
+ * 90-126 for 3D): d[axis] = iFFT(i xi FFT psi), dd = iFFT(-xi^2 FFT psi),
+ * rx = iFFT_x(i y xi_x FFT_x psi), ry = iFFT_y(-i x xi_y FFT_y psi).
+ * Outputs may be NULL.  Each non-NULL output holds total complex entries.
+ */
+int or_derivatives(int ndim, const int64_t *n, const double *lo, const double *hi,
+                   const double *psi, double *dx, double *dy, double *dz,
+                   double *ddx, double *ddy, double *ddz, double *rx, double *ry)
+{
+    ogrid g;
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    double *d1[3] = {dx, dy, dz}, *d2[3] = {ddx, ddy, ddz}, *rr[3] = {rx, ry, NULL};
+    const ocplx *p = (const ocplx *)psi;
+    int64_t nx = g.n[0], ny = g.n[1];
+    for (int a = 0; a < ndim; a++) {
+        int64_t len = g.n[a];
+        int64_t stride = a == 0 ? 1 : (a == 1 ? nx : nx * ny);
+        int64_t nlines = g.total / len;
+        double inv_n = 1.0 / (double)len;
+#pragma omp parallel
+        {
+            ocplx *hat = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+            ocplx *line = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+            ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+#pragma omp for schedule(static)
+            for (int64_t l = 0; l < nlines; l++) {
+                int64_t base = a == 0 ? l * nx : (a == 1 ? (l % nx) + (l / nx) * nx * ny : l);
+                double c = 0.0;
+                if (a == 0 && ndim >= 2) c = g.coord[1][l % ny];
+                if (a == 1) c = g.coord[0][l % nx];
+                for (int64_t q = 0; q < len; q++) hat[q] = p[base + q * stride];
+                fft_line(&g.plan[a], hat, tmp, -1);
+                for (int kind = 0; kind < 3; kind++) {
+                    double *out = kind == 0 ? d1[a] : (kind == 1 ? d2[a] : rr[a]);
+                    if (!out) continue;
+                    for (int64_t k = 0; k < len; k++) {
+                        double xi = g.xi[a][k], hr = hat[k].re, hi_ = hat[k].im;
+                        if (kind == 0) {        /* i xi hat */
+                            line[k].re = -xi * hi_; line[k].im = xi * hr;
+                        } else if (kind == 1) { /* -xi^2 hat */
+                            line[k].re = -(xi * xi) * hr; line[k].im = -(xi * xi) * hi_;
+                        } else if (a == 0) {    /* i y xi hat */
+                            line[k].re = -(c * xi) * hi_; line[k].im = (c * xi) * hr;
+                        } else {                /* -i x xi hat */
+                            line[k].re = (c * xi) * hi_; line[k].im = -(c * xi) * hr;
+                        }
+                    }
+                    fft_line(&g.plan[a], line, tmp, +1);
+                    ocplx *o = (ocplx *)out;
+                    for (int64_t q = 0; q < len; q++) {
+                        o[base + q * stride].re = line[q].re * inv_n;
+                        o[base + q * stride].im = line[q].im * inv_n;
+                    }
+                }
+            }
+            free(hat); free(line); free(tmp);
+        }
+    }
+    grid_free(&g);
+    return 0;
+}
+
+/*
+ * energy(n) of GrossPitaevskii.jl:61-92 (2D) / 106-136 (3D):
+ *   out[0] = E_Omega = sum Re(i conj(psi) Om (rx + ry)) dV
+ *   out[1] = E_Delta = (-cD (sum|dx|^2 + sum|dy|^2 [+ sum|dz|^2]) + sum V|psi|^2) dV
+ *   out[2] = E_beta  = sum 0.5 beta |psi|^4 dV
+ *   out[3] = E       = -E_Omega + E_Delta + E_beta
+ *   out[4] = mu      = -E_Omega + E_Delta + 2 E_beta  (GrossPitaevskii.jl:79;
+ *                      the 3D method computes no mu, the same formula is used)
+ */
+int or_energy(int ndim, const int64_t *n, const double *lo, const double *hi,
+              double cD, double beta, double Om, const double *V, const double *psi,
+              double *out)
+{
+    ogrid g;
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    int64_t N = g.total;
+    double *d[3] = {NULL, NULL, NULL}, *rx = NULL, *ry = NULL, *tmp = NULL;
+    int rc = -1;
+    for (int a = 0; a < ndim; a++) {
+        d[a] = (double *)malloc(sizeof(double) * 2 * (size_t)N);
+        if (!d[a]) goto done;
+    }
+    rx = (double *)calloc(2 * (size_t)N, sizeof(double));
+    ry = (double *)calloc(2 * (size_t)N, sizeof(double));
+    tmp = (double *)malloc(sizeof(double) * (size_t)N);
+    if (!rx || !ry || !tmp) goto done;
+    if (or_derivatives(ndim, n, lo, hi, psi, d[0], ndim > 1 ? d[1] : NULL, ndim > 2 ? d[2] : NULL,
+                       NULL, NULL, NULL, rx, ndim > 1 ? ry : NULL))
+        goto done;
+    const ocplx *p = (const ocplx *)psi;
+    double grad = 0.0;
+    for (int a = 0; a < ndim; a++) {
+        const ocplx *da = (const ocplx *)d[a];
+        for (int64_t i = 0; i < N; i++) tmp[i] = da[i].re * da[i].re + da[i].im * da[i].im;
+        grad += pairwise_sum(tmp, N);
+    }
+    const ocplx *X = (const ocplx *)rx, *Y = (const ocplx *)ry;
+    for (int64_t i = 0; i < N; i++) {
+        /* real(im * conj(psi) * (Om * (rx + ry))) */
+        double sr = Om * (X[i].re + Y[i].re), si = Om * (X[i].im + Y[i].im);
+        double cr = p[i].re, ci = -p[i].im;                 /* conj(psi) */
+        double pr = cr * sr - ci * si, pi_ = cr * si + ci * sr;
+        tmp[i] = -pi_;                                       /* real(i * z) = -imag(z) */
+        (void)pr;
+    }
+    double eom = times_cell(&g, pairwise_sum(tmp, N));
+    for (int64_t i = 0; i < N; i++) {
+        double r = p[i].re * p[i].re + p[i].im * p[i].im;
+        tmp[i] = (V ? V[i] : 0.0) * r;
+    }
+    double epot = pairwise_sum(tmp, N);
+    double edel = times_cell(&g, -cD * grad + epot);
+    for (int64_t i = 0; i < N; i++) {
+        double r = p[i].re * p[i].re + p[i].im * p[i].im;
+        tmp[i] = (0.5 * beta) * (r * r);
+    }
+    double ebeta = times_cell(&g, pairwise_sum(tmp, N));
+    out[0] = eom;
+    out[1] = edel;
+    out[2] = ebeta;
+    out[3] = -eom + edel + ebeta;
+    out[4] = -eom + edel + ebeta * 2.0;
+    rc = 0;
+done:
+    for (int a = 0; a < 3; a++) free(d[a]);
+    free(rx); free(ry); free(tmp);
+    grid_free(&g);
+    return rc;
+}
+
+int or_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

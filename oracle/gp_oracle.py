@@ -1,0 +1,230 @@
+"""CPU oracle for the split-step Gross-Pitaevskii path -- TEST INFRASTRUCTURE ONLY.
+
+Two independent FP64 restatements of SuperfluidDynamics.jl's `NumModelSplit1` /
+`NumModelSplit2` path (src/NumModels/GrossPitaevskii/splitting.jl:78-82, 149-209):
+
+* ``C*`` functions wrap ``gp_oracle.c`` (own radix-2 FFT, OpenMP), compiled by
+  ``oracle/Makefile`` into ``oracle/_build/libgporacle.so``;
+* ``np_*`` functions restate the same stages with ``numpy.fft`` (pocketfft), a
+  second FFT implementation, for small cross-checks.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline arm use
+this module, and only as the checker.  Fields are numpy arrays of shape
+``(nx, ny[, nz])`` in Fortran order, i.e. x fastest in memory like the
+reference's Julia ``Array{ComplexF64}``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libgporacle.so")
+_lib = None
+
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile gp_oracle.c with oracle/Makefile; returns the library path."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.or_grid_coords.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, _f64p]
+        L.or_fftfreq.argtypes = [ctypes.c_int64, ctypes.c_double, _f64p]
+        L.or_norm.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p]
+        L.or_norm.restype = ctypes.c_double
+        L.or_fft_axis.argtypes = [ctypes.c_int, _i64p, _f64p, ctypes.c_int, ctypes.c_int]
+        L.or_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
+                              ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
+                              ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.or_derivatives.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p] + [_f64p] * 8
+        L.or_energy.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_double, _f64p, _f64p, _f64p]
+        L.or_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_f64p)
+
+
+def _geom(shape, bounds):
+    nd = len(shape)
+    n = np.array(list(shape) + [1] * (3 - nd), dtype=np.int64)
+    lo = np.array([b[0] for b in bounds] + [0.0] * (3 - nd), dtype=np.float64)
+    hi = np.array([b[1] for b in bounds] + [1.0] * (3 - nd), dtype=np.float64)
+    return nd, n, lo, hi
+
+
+def _field(psi):
+    a = np.asfortranarray(psi, dtype=np.complex128)
+    return a
+
+
+# ------------------------------------------------------------------ grid --
+def grid_coords(n: int, lo: float, hi: float) -> np.ndarray:
+    """Grids.jl:78-84 node positions (LinRange(lo, hi, n+1)[1:end-1])."""
+    out = np.empty(n, dtype=np.float64)
+    lib().or_grid_coords(n, float(lo), float(hi), _p(out))
+    return out
+
+
+def fftfreq(n: int, d: float) -> np.ndarray:
+    """Plans.jl:829-830 wavenumbers fftfreq(n, 2pi/d)."""
+    out = np.empty(n, dtype=np.float64)
+    lib().or_fftfreq(n, float(d), _p(out))
+    return out
+
+
+def spacing(shape, bounds):
+    return [(b[1] - b[0]) / n for n, b in zip(shape, bounds)]
+
+
+def quadratic_potential(shape, bounds, gammas=None, alpha=0.0):
+    """PotentialQuadratic (src/Potentials/quadratic.jl:61-67):
+    V = 0.5 (1 - alpha) (gx x^2 + gy y^2 [+ gz z^2]), evaluated in Julia's order."""
+    nd = len(shape)
+    gammas = gammas or [1.0] * nd
+    xs = [grid_coords(n, b[0], b[1]) for n, b in zip(shape, bounds)]
+    grids = np.meshgrid(*xs, indexing="ij")
+    acc = gammas[0] * grids[0] ** 2
+    for a in range(1, nd):
+        acc = acc + gammas[a] * grids[a] ** 2
+    return np.asfortranarray(0.5 * (1 - alpha) * acc)
+
+
+# ---------------------------------------------------------------- C path --
+def c_norm(psi, bounds) -> float:
+    psi = _field(psi)
+    nd, n, lo, hi = _geom(psi.shape, bounds)
+    return lib().or_norm(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), _p(psi))
+
+
+def c_fft_axis(psi, axis: int, inverse: bool = False):
+    out = _field(psi).copy(order="F")
+    nd, n, lo, hi = _geom(out.shape, [(0, 1)] * out.ndim)
+    rc = lib().or_fft_axis(nd, n.ctypes.data_as(_i64p), _p(out), axis,
+                           1 if inverse else 0)
+    assert rc == 0
+    return out
+
+
+def c_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, scheme=2,
+           imag=False, dt=1e-3, nthreads=0):
+    """nsteps of NumModelSplit2 (scheme=2) or NumModelSplit1 (scheme=1); returns a new array."""
+    out = _field(psi).copy(order="F")
+    nd, n, lo, hi = _geom(out.shape, bounds)
+    Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
+    rc = lib().or_step(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
+                       _p(Vp), _p(out), int(nsteps), int(scheme),
+                       1 if imag else 0, float(dt), int(nthreads))
+    if rc != 0:
+        raise ValueError("or_step failed")
+    return out
+
+
+def c_derivatives(psi, bounds):
+    """computeDerivatives!(GradientRotField) -> dict of dx, dy, [dz], ddx, ..., rx, ry."""
+    psi = _field(psi)
+    nd, n, lo, hi = _geom(psi.shape, bounds)
+    names = ["dx", "dy", "dz", "ddx", "ddy", "ddz", "rx", "ry"]
+    outs = {}
+    ptrs = []
+    for nm in names:
+        axis = {"x": 0, "y": 1, "z": 2}[nm[-1]]
+        if axis < nd and not (nm.startswith("r") and nd < 2):
+            outs[nm] = np.zeros(psi.shape, dtype=np.complex128, order="F")
+            ptrs.append(_p(outs[nm]))
+        else:
+            ptrs.append(None)
+    rc = lib().or_derivatives(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi),
+                              _p(psi), *ptrs)
+    assert rc == 0
+    return outs
+
+
+def c_energy(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None):
+    """energy(n) of GrossPitaevskii.jl:61-136 -> (E_Omega, E_Delta, E_beta, E, mu)."""
+    psi = _field(psi)
+    nd, n, lo, hi = _geom(psi.shape, bounds)
+    out = np.zeros(5, dtype=np.float64)
+    Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
+    rc = lib().or_energy(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
+                         _p(Vp), _p(psi), _p(out))
+    assert rc == 0
+    return tuple(float(v) for v in out)
+
+
+def max_threads() -> int:
+    return int(lib().or_max_threads())
+
+
+# ------------------------------------------------------------ numpy path --
+def np_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, scheme=2,
+            imag=False, dt=1e-3):
+    """Same stages as c_step, with numpy.fft as the (independent) transform."""
+    p = np.array(psi, dtype=np.complex128, order="F", copy=True)
+    nd = p.ndim
+    shape = p.shape
+    d = spacing(shape, bounds)
+    xs = [grid_coords(n, b[0], b[1]) for n, b in zip(shape, bounds)]
+    xis = [fftfreq(n, dd) for n, dd in zip(shape, d)]
+    Vv = None if V is None else np.asarray(V, dtype=np.float64)
+
+    def bshape(v, axis):
+        s = [1] * nd
+        s[axis] = v.size
+        return v.reshape(s)
+
+    def lap(dtl):
+        for a in range(nd):
+            xi = bshape(xis[a], a)
+            if a == 0 and nd >= 2:
+                ph = coeffD * (xi * xi) - omega * bshape(xs[1], 1) * xi
+            elif a == 1:
+                ph = coeffD * (xi * xi) + omega * bshape(xs[0], 0) * xi
+            else:
+                ph = coeffD * (xi * xi)
+            fac = np.exp(ph * dtl) if imag else np.exp(1j * (ph * dtl))
+            p[...] = np.fft.ifft(fac * np.fft.fft(p, axis=a), axis=a)
+
+    def nl(dtl):
+        r = (0.0 if Vv is None else Vv) + beta * (p.real ** 2 + p.imag ** 2)
+        fac = np.exp(-r * dtl) if imag else np.exp(1j * (-r * dtl))
+        p[...] = fac * p
+
+    for _ in range(nsteps):
+        if scheme == 2:
+            lap(dt * 0.5); nl(dt); lap(dt * 0.5)
+        else:
+            lap(dt); nl(dt)
+        if imag:
+            nrm = np.sqrt(np.sum(np.abs(p) ** 2)) * np.sqrt(np.prod(d))
+            p /= nrm
+    return p
+
+
+def rel_l2(a, b) -> float:
+    """Relative L2 distance ||a-b|| / ||b|| (the reference's GPU test metric,
+    test/runtests.jl:1416-1417)."""
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.sqrt(np.sum(np.abs(a - b) ** 2)) / np.sqrt(np.sum(np.abs(b) ** 2)))
+
+
+def relerr_max(a, b) -> float:
+    """Max-norm relative error, test/runtests.jl:5."""
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))

@@ -1,0 +1,852 @@
+// gpss_api.cu -- the C ABI of libgpss.so (include/gpss.h): context setup,
+// host-built FP64 tables, and the orchestration of the directional passes
+// that make up NumModelSplit1 / NumModelSplit2 time steps.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include "../../include/gpss.h"
+#include "gpss_internal.h"
+
+using namespace gpss;
+
+#define GPSS_VERSION_STRING "gpss 0.1.0 (sm_103a)"
+
+static const double kTwoPi = 6.283185307179586;  // Float64(2pi)
+
+struct PhaseEntry {
+    int axis, imag, fused;
+    double dtl, cD, om;
+    void *dev;
+    int64_t prow;
+};
+
+struct gpss_ctx {
+    int ndim = 0;
+    int64_t n[3] = {1, 1, 1};
+    double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1}, L[3] = {1, 1, 1}, d[3] = {1, 1, 1};
+    int64_t total = 0;
+    int precision = GPSS_FP64;
+    int flags = 0;
+    double cD = -0.5, beta = 1.0, omega = 0.0;
+    bool have_psi = false;
+    bool have_V = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void *psi = nullptr;      // device field (float2 or double2)
+    void *scratch = nullptr;  // spectrum (plain form) and FP64 staging, total*16 bytes
+    void *V = nullptr;        // device potential (float or double)
+    void *tw[3] = {nullptr, nullptr, nullptr};
+    double *coord_dev[3] = {nullptr, nullptr, nullptr};
+    std::vector<double> coord[3];
+    double *partials = nullptr;
+    int max_blocks = 0;
+    double *sums = nullptr;   // [4][RQ_COUNT]
+    double *scale = nullptr;  // [1]
+    int *status = nullptr;    // [1]
+    std::vector<PhaseEntry> phases;
+    cudaEvent_t ev[8] = {};
+    int64_t launches = 0;
+    int64_t bytes = 0;
+    std::string err;
+};
+
+static thread_local std::string g_create_error;
+
+static int fail(gpss_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_create_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(c, call)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail((c), GPSS_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
+    } while (0)
+
+#define GPSS_TRY(call)            \
+    do {                          \
+        int rc_ = (call);         \
+        if (rc_ != GPSS_OK)       \
+            return rc_;           \
+    } while (0)
+
+static int dev_alloc(gpss_ctx *c, void **p, size_t bytes)
+{
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(c, GPSS_ENOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    c->bytes += (int64_t)bytes;
+    return GPSS_OK;
+}
+
+// (cos, sin) of 2 pi k / n, reduced to the first octant so that the
+// symmetric values are exact.
+static void unit_root(int64_t k, int64_t n, double *cs, double *sn)
+{
+    k %= n;
+    if (k < 0) k += n;
+    int64_t q = (4 * k) / n;
+    int64_t r4 = 4 * k - q * n;
+    double cc, ss;
+    if (2 * r4 <= n) {
+        double a = 0.5 * M_PI * (double)r4 / (double)n;
+        cc = std::cos(a); ss = std::sin(a);
+    } else {
+        double a = 0.5 * M_PI * (double)(n - r4) / (double)n;
+        cc = std::sin(a); ss = std::cos(a);
+    }
+    switch (q) {
+    case 0: *cs = cc; *sn = ss; break;
+    case 1: *cs = -ss; *sn = cc; break;
+    case 2: *cs = -cc; *sn = -ss; break;
+    default: *cs = ss; *sn = -cc; break;
+    }
+}
+
+// Grids.jl:78-84: x = LinRange(lo, hi, n+1)[1:end-1] (lerps of Base.LinRange)
+static double lerpi(int64_t j, int64_t dd, double a, double b)
+{
+    double t = (double)j / (double)dd;
+    return (1.0 - t) * a + t * b;
+}
+
+static void grid_coords(int64_t n, double lo, double hi, std::vector<double> &x)
+{
+    x.resize((size_t)n);
+    if (n <= 1) { x[0] = lo; return; }
+    double first = lerpi(0, n, lo, hi), last = lerpi(n - 1, n, lo, hi);
+    for (int64_t i = 0; i < n; i++) x[(size_t)i] = lerpi(i, n - 1, first, last);
+}
+
+// Plans.jl:829-830: xi_k = kk * ((2pi/dx)/n), kk the signed index of fftfreq
+static double xi_mult(const gpss_ctx *c, int axis) { return (kTwoPi / c->d[axis]) / (double)c->n[axis]; }
+static double xi_of(const gpss_ctx *c, int axis, int64_t k)
+{
+    int64_t n = c->n[axis];
+    int64_t kk = k < (n + 1) / 2 ? k : k - n;
+    return (double)kk * xi_mult(c, axis);
+}
+
+static size_t cplx_bytes(const gpss_ctx *c) { return c->precision == GPSS_FP32 ? 8 : 16; }
+static size_t real_bytes(const gpss_ctx *c) { return c->precision == GPSS_FP32 ? 4 : 8; }
+
+// upload n doubles as T
+static int upload_table(gpss_ctx *c, void **dev, const std::vector<double> &h)
+{
+    size_t cnt = h.size();
+    GPSS_TRY(dev_alloc(c, dev, cnt * real_bytes(c)));
+    if (c->precision == GPSS_FP32) {
+        std::vector<float> f(cnt);
+        for (size_t i = 0; i < cnt; i++) f[i] = (float)h[i];
+        CUDA_TRY(c, cudaMemcpy(*dev, f.data(), cnt * 4, cudaMemcpyHostToDevice));
+    } else {
+        CUDA_TRY(c, cudaMemcpy(*dev, h.data(), cnt * 8, cudaMemcpyHostToDevice));
+    }
+    return GPSS_OK;
+}
+
+// Kinetic factor table for `axis` (splitting.jl:167/172/190/195/200):
+// real time  exp(i (cD xi^2 -/+ Om c xi) dtl), imaginary time exp((...) dtl);
+// fused tables also carry the 1/n of the inverse transform.  With Omega != 0
+// the x (y) table has one row per y (x) node.
+static int get_phase(gpss_ctx *c, int axis, double dtl, int imag, int fused, const void **dev,
+                     int64_t *prow)
+{
+    for (auto &e : c->phases) {
+        if (e.axis == axis && e.dtl == dtl && e.imag == imag && e.fused == fused && e.cD == c->cD &&
+            e.om == c->omega) {
+            *dev = e.dev;
+            *prow = e.prow;
+            return GPSS_OK;
+        }
+    }
+    const int64_t n = c->n[axis];
+    const bool rot = c->omega != 0.0 && axis < 2 && c->ndim >= 2;
+    const int64_t rows = rot ? (axis == 0 ? c->n[1] : c->n[0]) : 1;
+    std::vector<double> h((size_t)(2 * n * rows));
+    const double inv_n = fused ? 1.0 / (double)n : 1.0;
+    for (int64_t r = 0; r < rows; r++) {
+        const double cr = rot ? (axis == 0 ? c->coord[1][(size_t)r] : c->coord[0][(size_t)r]) : 0.0;
+        for (int64_t k = 0; k < n; k++) {
+            const double xk = xi_of(c, axis, k);
+            double ph;
+            if (axis == 0) ph = c->cD * (xk * xk) - c->omega * cr * xk;
+            else if (axis == 1) ph = c->cD * (xk * xk) + c->omega * cr * xk;
+            else ph = c->cD * (xk * xk);
+            double fr, fi;
+            if (!imag) { double t = ph * dtl; fr = std::cos(t); fi = std::sin(t); }
+            else { fr = std::exp(ph * dtl); fi = 0.0; }
+            h[(size_t)(2 * (k + r * n))] = fr * inv_n;
+            h[(size_t)(2 * (k + r * n) + 1)] = fi * inv_n;
+        }
+    }
+    PhaseEntry e{axis, imag, fused, dtl, c->cD, c->omega, nullptr, rot ? n : 0};
+    GPSS_TRY(upload_table(c, &e.dev, h));
+    if (c->phases.size() > 64) {  // bounded cache: drop the oldest
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->phases.front().dev);
+        c->phases.erase(c->phases.begin());
+    }
+    c->phases.push_back(e);
+    *dev = e.dev;
+    *prow = e.prow;
+    return GPSS_OK;
+}
+
+static void clear_phases(gpss_ctx *c)
+{
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &e : c->phases) cudaFree(e.dev);
+    c->phases.clear();
+}
+
+template <typename T> static PassArgs<T> axis_args(gpss_ctx *c, int axis, const void *in, void *out)
+{
+    PassArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    const int64_t nx = c->n[0], ny = c->n[1];
+    const int64_t n = c->n[axis];
+    a.in = (const vec2<T> *)in;
+    a.out = (vec2<T> *)out;
+    a.tw = (const vec2<T> *)c->tw[axis];
+    a.nlines = (int)(c->total / n);
+    if (axis == 0) { a.m0 = a.nlines; a.s0 = nx; a.s1 = 0; a.stride = 1; a.rowmod = (int)ny; }
+    else if (axis == 1) { a.m0 = (int)nx; a.s0 = 1; a.s1 = nx * ny; a.stride = nx; a.rowmod = (int)nx; }
+    else { a.m0 = a.nlines; a.s0 = 1; a.s1 = 0; a.stride = nx * ny; a.rowmod = 1; }
+    a.inv_n = (T)(1.0 / (double)n);
+    a.kmult = xi_mult(c, axis);
+    a.nl_mode = NL_NONE;
+    return a;
+}
+
+template <typename T> static int blocks_for(gpss_ctx *c, int axis)
+{
+    const int W = PassLauncher<T>::lines((int)c->n[axis], axis == 0);
+    const int64_t nl = c->total / c->n[axis];
+    return (int)((nl + W - 1) / W);
+}
+
+template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const PassArgs<T> &a)
+{
+    const int blocks = blocks_for<T>(c, axis);
+    cudaError_t e = PassLauncher<T>::launch(mode, axis == 0, (int)c->n[axis], a, blocks, c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "pass launch (axis %d, mode %d): %s", axis, mode,
+                                      cudaGetErrorString(e));
+    c->launches++;
+    return GPSS_OK;
+}
+
+static int finalize(gpss_ctx *c, int axis_blocks, int slot, int renorm)
+{
+    double dV = 1.0;
+    for (int a = 0; a < c->ndim; a++) dV *= c->d[a];
+    cudaError_t e = launch_finalize(c->partials, axis_blocks, RQ_COUNT, c->sums + slot * RQ_COUNT,
+                                    renorm, dV, c->scale, c->status, c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "finalize launch: %s", cudaGetErrorString(e));
+    c->launches++;
+    return GPSS_OK;
+}
+
+// One kinetic flow L(dtl) as fused passes x, y[, z].  The last axis may carry
+// the nonlinear flow N(dtnl) as an epilogue and/or the pointwise reductions
+// (red_last); diag_kin adds the Parseval kinetic sums on every axis;
+// prescale multiplies the first pass's input by the device scalar c->scale.
+template <typename T>
+static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl, int red_last,
+                         bool diag_kin, bool prescale)
+{
+    for (int axis = 0; axis < c->ndim; axis++) {
+        PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
+        const void *ph;
+        GPSS_TRY(get_phase(c, axis, dtl, imag, 1, &ph, &a.prow));
+        a.phase = (const vec2<T> *)ph;
+        if (prescale && axis == 0) a.scale = c->scale;
+        const bool last = axis == c->ndim - 1;
+        if (last && nl) {
+            a.nl_mode = imag ? NL_IMAG : NL_REAL;
+            a.V = c->have_V ? (const T *)c->V : nullptr;
+            a.nl_beta = c->beta;
+            a.nl_dt = dtnl;
+        }
+        if (last) a.red |= red_last;
+        if (a.red & RED_POINT) a.V = c->have_V ? (const T *)c->V : nullptr;
+        if (diag_kin) {
+            a.red |= RED_KIN;
+            a.coord = axis == 0 ? c->coord_dev[1] : (axis == 1 ? c->coord_dev[0] : nullptr);
+        }
+        if (a.red) a.partials = c->partials;
+        GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
+        if (a.red) GPSS_TRY(finalize(c, blocks_for<T>(c, axis), axis, imag && last && (red_last & RED_POINT)));
+    }
+    return GPSS_OK;
+}
+
+// Plain form: per axis FFT -> multiply -> iFFT as three launches
+// (mul_x!, broadcast, ldiv_x!; Plans.jl:1132-1250, splitting.jl:164-201).
+template <typename T> static int kinetic_plain(gpss_ctx *c, double dtl, int imag)
+{
+    for (int axis = 0; axis < c->ndim; axis++) {
+        PassArgs<T> f = axis_args<T>(c, axis, c->psi, c->scratch);
+        GPSS_TRY(launch<T>(c, axis, MODE_FWD, f));
+        const void *ph;
+        int64_t prow;
+        GPSS_TRY(get_phase(c, axis, dtl, imag, 0, &ph, &prow));
+        cudaError_t e = launch_mul_phase<T>((vec2<T> *)c->scratch, (const vec2<T> *)ph, prow, axis, c->n,
+                                            c->total, c->stream);
+        if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "mul_phase: %s", cudaGetErrorString(e));
+        c->launches++;
+        PassArgs<T> b = axis_args<T>(c, axis, c->scratch, c->psi);
+        GPSS_TRY(launch<T>(c, axis, MODE_INV, b));
+    }
+    return GPSS_OK;
+}
+
+template <typename T> static int nl_plain(gpss_ctx *c, double dt, int imag)
+{
+    cudaError_t e = launch_nl<T>((vec2<T> *)c->psi, c->have_V ? (const T *)c->V : nullptr, c->beta, dt, imag,
+                                 c->total, c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl: %s", cudaGetErrorString(e));
+    c->launches++;
+    return GPSS_OK;
+}
+
+// sum |psi|^2 (and V|psi|^2, |psi|^4; with kin also the Parseval sums) of the
+// current field, read-only passes, into c->sums[slot axis]
+template <typename T> static int diag_passes(gpss_ctx *c, bool kin, int renorm)
+{
+    const int naxes = kin ? c->ndim : 1;
+    for (int axis = 0; axis < naxes; axis++) {
+        PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
+        a.red = (axis == 0 ? RED_POINT : 0) | (kin ? RED_KIN : 0);
+        a.V = c->have_V ? (const T *)c->V : nullptr;
+        a.coord = axis == 0 ? c->coord_dev[1] : (axis == 1 ? c->coord_dev[0] : nullptr);
+        a.partials = c->partials;
+        GPSS_TRY(launch<T>(c, axis, MODE_DIAG, a));
+        GPSS_TRY(finalize(c, blocks_for<T>(c, axis), axis, renorm && axis == 0));
+    }
+    return GPSS_OK;
+}
+
+template <typename T> static int apply_scale(gpss_ctx *c)
+{
+    cudaError_t e = launch_scale<T>((vec2<T> *)c->psi, c->scale, c->total, c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "scale: %s", cudaGetErrorString(e));
+    c->launches++;
+    return GPSS_OK;
+}
+
+static double cell_volume(const gpss_ctx *c)
+{
+    double v = 1.0;
+    for (int a = 0; a < c->ndim; a++) v *= c->d[a];
+    return v;
+}
+
+// x * dx * dy [* dz] left to right, as the reference evaluates it
+static double times_cell(const gpss_ctx *c, double x)
+{
+    for (int a = 0; a < c->ndim; a++) x *= c->d[a];
+    return x;
+}
+
+// energies from the per-axis sums (slot a holds the sums of the axis-a pass)
+static void energies_from_sums(const gpss_ctx *c, const double *h, int point_slot, double *out)
+{
+    const double *pt = h + point_slot * RQ_COUNT;
+    double grad = 0.0;
+    for (int a = 0; a < c->ndim; a++) grad += h[a * RQ_COUNT + RQ_KIN];
+    // sum Re(i conj(psi) Om (rx + ry)) = -Om (rot_x - rot_y) by Parseval on x and y lines
+    const double rotx = h[0 * RQ_COUNT + RQ_ROT];
+    const double roty = c->ndim >= 2 ? h[1 * RQ_COUNT + RQ_ROT] : 0.0;
+    const double eom = times_cell(c, -c->omega * (rotx - roty));
+    const double edel = times_cell(c, -c->cD * grad + pt[RQ_POT]);
+    const double ebeta = times_cell(c, 0.5 * c->beta * pt[RQ_INT]);
+    out[0] = eom;
+    out[1] = edel;
+    out[2] = ebeta;
+    out[3] = -eom + edel + ebeta;
+    out[4] = -eom + edel + ebeta * 2.0;
+}
+
+static int read_sums(gpss_ctx *c, double *h)
+{
+    CUDA_TRY(c, cudaMemcpyAsync(h, c->sums, sizeof(double) * 4 * RQ_COUNT, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GPSS_OK;
+}
+
+template <typename T> static int energy_impl(gpss_ctx *c, double *out, double *mass)
+{
+    GPSS_TRY(diag_passes<T>(c, true, 0));
+    double h[4 * RQ_COUNT];
+    GPSS_TRY(read_sums(c, h));
+    if (!std::isfinite(h[RQ_MASS])) return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
+    if (out) energies_from_sums(c, h, 0, out);
+    if (mass) *mass = times_cell(c, h[RQ_MASS]);
+    return GPSS_OK;
+}
+
+template <typename T>
+static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_diag *diag)
+{
+    const bool plain = (c->flags & GPSS_FLAG_PLAIN) != 0;
+    const bool merge = !plain && !imag && scheme == GPSS_STRANG && c->omega == 0.0 &&
+                       !(c->flags & GPSS_FLAG_NOMERGE);
+    bool diag_done = false;
+    if (nsteps == 0) {
+        if (diag) {
+            diag->steps = 0;
+            GPSS_TRY(energy_impl<T>(c, diag->energy, &diag->mass));
+        }
+        return GPSS_OK;
+    }
+    if (imag) {
+        int zero = 0;
+        CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    }
+    if (plain) {
+        for (int s = 0; s < nsteps; s++) {
+            if (scheme == GPSS_STRANG) {
+                GPSS_TRY(kinetic_plain<T>(c, dt * 0.5, imag));
+                GPSS_TRY(nl_plain<T>(c, dt, imag));
+                GPSS_TRY(kinetic_plain<T>(c, dt * 0.5, imag));
+            } else {
+                GPSS_TRY(kinetic_plain<T>(c, dt, imag));
+                GPSS_TRY(nl_plain<T>(c, dt, imag));
+            }
+            if (imag) {  // normalize! (Fields.jl:196-200)
+                GPSS_TRY(diag_passes<T>(c, false, 1));
+                GPSS_TRY(apply_scale<T>(c));
+            }
+        }
+    } else if (merge) {
+        // L(dt/2) N [L(dt) N]^(nsteps-1) L(dt/2): the kinetic flows of
+        // consecutive steps commute (Omega = 0) and compose exactly.
+        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, 0, false, false));
+        for (int s = 1; s < nsteps; s++) GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, 0, false, false));
+        // final half step; with diag, the kinetic sums of each axis are exact
+        // for the final field (real-time kinetic flows are unitary and commute
+        // with the other axes' derivatives when Omega = 0)
+        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, diag ? RED_POINT : 0, diag != nullptr, false));
+        diag_done = diag != nullptr;
+    } else {
+        for (int s = 0; s < nsteps; s++) {
+            const bool pre = imag && s > 0;
+            if (scheme == GPSS_STRANG) {
+                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, imag, true, dt, 0, false, pre));
+                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, imag, false, 0.0, imag ? RED_POINT : 0, false, false));
+            } else {
+                GPSS_TRY(kinetic_fused<T>(c, dt, imag, true, dt, imag ? RED_POINT : 0, false, pre));
+            }
+        }
+        if (imag && nsteps > 0) GPSS_TRY(apply_scale<T>(c));
+    }
+    if (imag) {
+        int st = 0;
+        CUDA_TRY(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if (st) return fail(c, GPSS_ENONFINITE, "imaginary-time renormalisation saw a non-finite or zero mass");
+    }
+    if (diag) {
+        diag->steps = nsteps;
+        if (diag_done) {
+            double h[4 * RQ_COUNT];
+            GPSS_TRY(read_sums(c, h));
+            const int last = c->ndim - 1;
+            if (!std::isfinite(h[last * RQ_COUNT + RQ_MASS]))
+                return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
+            energies_from_sums(c, h, last, diag->energy);
+            diag->mass = times_cell(c, h[last * RQ_COUNT + RQ_MASS]);
+        } else {
+            GPSS_TRY(energy_impl<T>(c, diag->energy, &diag->mass));
+        }
+    }
+    return GPSS_OK;
+}
+
+static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+
+extern "C" {
+
+const char *gpss_version(void) { return GPSS_VERSION_STRING; }
+
+const char *gpss_last_error(const gpss_ctx *ctx)
+{
+    if (!ctx) return g_create_error.c_str();
+    return ctx->err.c_str();
+}
+
+void gpss_destroy(gpss_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    clear_phases(c);
+    void *ptrs[] = {c->psi, c->scratch, c->V, c->tw[0], c->tw[1], c->tw[2], c->coord_dev[0],
+                    c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, const double *hi,
+                int precision, int flags)
+{
+    if (!out || !n || !lo || !hi) return fail(nullptr, GPSS_EINVAL, "gpss_create: null argument");
+    *out = nullptr;
+    if (ndim != 2 && ndim != 3) return fail(nullptr, GPSS_EINVAL, "ndim must be 2 or 3 (got %d)", ndim);
+    if (precision != GPSS_FP64 && precision != GPSS_FP32)
+        return fail(nullptr, GPSS_EINVAL, "precision must be GPSS_FP64 or GPSS_FP32 (got %d)", precision);
+    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE))
+        return fail(nullptr, GPSS_EINVAL, "unknown flags 0x%x", flags);
+    for (int a = 0; a < ndim; a++) {
+        if (!is_pow2(n[a]) || n[a] < 2 || n[a] > 256)
+            return fail(nullptr, GPSS_EINVAL, "n[%d] = %lld: each axis must be a power of two in [2, 256]", a,
+                        (long long)n[a]);
+        if (!(hi[a] > lo[a]) || !std::isfinite(lo[a]) || !std::isfinite(hi[a]))
+            return fail(nullptr, GPSS_EINVAL, "axis %d: need finite lo < hi", a);
+    }
+    gpss_ctx *c = new (std::nothrow) gpss_ctx();
+    if (!c) return fail(nullptr, GPSS_ENOMEM, "host allocation failed");
+    c->ndim = ndim;
+    c->precision = precision;
+    c->flags = flags;
+    c->total = 1;
+    for (int a = 0; a < 3; a++) {
+        c->n[a] = a < ndim ? n[a] : 1;
+        c->lo[a] = a < ndim ? lo[a] : 0.0;
+        c->hi[a] = a < ndim ? hi[a] : 1.0;
+        c->L[a] = c->hi[a] - c->lo[a];
+        c->d[a] = c->L[a] / (double)c->n[a];
+        c->total *= c->n[a];
+        grid_coords(c->n[a], c->lo[a], c->hi[a], c->coord[a]);
+    }
+    auto bail = [&](int rc) {
+        g_create_error = c->err;
+        gpss_destroy(c);
+        return rc;
+    };
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
+    for (auto &ev : c->ev) {
+        e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaEventCreate: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
+    }
+    int rc;
+    if ((rc = dev_alloc(c, &c->psi, (size_t)c->total * cplx_bytes(c)))) return bail(rc);
+    if ((rc = dev_alloc(c, &c->scratch, (size_t)c->total * 16))) return bail(rc);
+    // twiddles per axis, stage-A layout tw[k1*N2 + r] = exp(-2 pi i r k1 / n)
+    for (int a = 0; a < ndim; a++) {
+        const int64_t na = c->n[a];
+        const int64_t N1 = na <= 16 ? na : 16, N2 = na / N1;
+        std::vector<double> h((size_t)(2 * na));
+        for (int64_t k1 = 0; k1 < N1; k1++)
+            for (int64_t r = 0; r < N2; r++) {
+                double cs, sn;
+                unit_root(r * k1, na, &cs, &sn);
+                h[(size_t)(2 * (k1 * N2 + r))] = cs;
+                h[(size_t)(2 * (k1 * N2 + r) + 1)] = -sn;
+            }
+        if ((rc = upload_table(c, &c->tw[a], h))) return bail(rc);
+        if ((rc = dev_alloc(c, (void **)&c->coord_dev[a], sizeof(double) * (size_t)c->n[a]))) return bail(rc);
+        e = cudaMemcpy(c->coord_dev[a], c->coord[a].data(), sizeof(double) * (size_t)c->n[a], cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
+    }
+    int maxb = 1;
+    for (int a = 0; a < ndim; a++) {
+        int b = precision == GPSS_FP32 ? blocks_for<float>(c, a) : blocks_for<double>(c, a);
+        if (b > maxb) maxb = b;
+    }
+    c->max_blocks = maxb;
+    if ((rc = dev_alloc(c, (void **)&c->partials, sizeof(double) * RQ_COUNT * (size_t)maxb))) return bail(rc);
+    if ((rc = dev_alloc(c, (void **)&c->sums, sizeof(double) * 4 * RQ_COUNT))) return bail(rc);
+    if ((rc = dev_alloc(c, (void **)&c->scale, sizeof(double) * 2))) return bail(rc);
+    if ((rc = dev_alloc(c, (void **)&c->status, sizeof(int) * 2))) return bail(rc);
+    double one = 1.0;
+    e = cudaMemcpy(c->scale, &one, sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
+    *out = c;
+    return GPSS_OK;
+}
+
+int gpss_set_params(gpss_ctx *c, double coeffD, double beta, double omega)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!std::isfinite(coeffD) || !std::isfinite(beta) || !std::isfinite(omega))
+        return fail(c, GPSS_EINVAL, "parameters must be finite");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (coeffD != c->cD || omega != c->omega) clear_phases(c);
+    c->cD = coeffD;
+    c->beta = beta;
+    c->omega = omega;
+    return GPSS_OK;
+}
+
+int gpss_set_potential(gpss_ctx *c, const double *V)
+{
+    if (!c) return GPSS_EINVAL;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!V) { c->have_V = false; return GPSS_OK; }
+    if (!c->V) GPSS_TRY(dev_alloc(c, &c->V, (size_t)c->total * real_bytes(c)));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (c->precision == GPSS_FP64) {
+        CUDA_TRY(c, cudaMemcpyAsync(c->V, V, (size_t)c->total * 8, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        CUDA_TRY(c, cudaMemcpyAsync(c->scratch, V, (size_t)c->total * 8, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, launch_f64_to_f32((const double *)c->scratch, (float *)c->V, c->total, c->stream));
+        c->launches++;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->have_V = true;
+    return GPSS_OK;
+}
+
+int gpss_upload(gpss_ctx *c, const double *psi)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!psi) return fail(c, GPSS_EINVAL, "gpss_upload: null psi");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (c->precision == GPSS_FP64) {
+        CUDA_TRY(c, cudaMemcpyAsync(c->psi, psi, (size_t)c->total * 16, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        CUDA_TRY(c, cudaMemcpyAsync(c->scratch, psi, (size_t)c->total * 16, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, launch_f64_to_f32((const double *)c->scratch, (float *)c->psi, 2 * c->total, c->stream));
+        c->launches++;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->have_psi = true;
+    return GPSS_OK;
+}
+
+int gpss_download(gpss_ctx *c, double *psi)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!psi) return fail(c, GPSS_EINVAL, "gpss_download: null psi");
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (c->precision == GPSS_FP64) {
+        CUDA_TRY(c, cudaMemcpyAsync(psi, c->psi, (size_t)c->total * 16, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        CUDA_TRY(c, launch_f32_to_f64((const float *)c->psi, (double *)c->scratch, 2 * c->total, c->stream));
+        c->launches++;
+        CUDA_TRY(c, cudaMemcpyAsync(psi, c->scratch, (size_t)c->total * 16, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GPSS_OK;
+}
+
+int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_diag *diag)
+{
+    if (!c) return GPSS_EINVAL;
+    if (nsteps < 0) return fail(c, GPSS_EINVAL, "nsteps must be >= 0");
+    if (scheme != GPSS_LIE && scheme != GPSS_STRANG) return fail(c, GPSS_EINVAL, "scheme must be 1 (Lie) or 2 (Strang)");
+    if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "dt must be finite");
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (nsteps == 0 && !diag) return GPSS_OK;
+    if (c->precision == GPSS_FP32) return step_impl<float>(c, nsteps, scheme, imag, dt, diag);
+    return step_impl<double>(c, nsteps, scheme, imag, dt, diag);
+}
+
+int gpss_energy(gpss_ctx *c, double *out)
+{
+    if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_energy: null out") : GPSS_EINVAL;
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (c->precision == GPSS_FP32) return energy_impl<float>(c, out, nullptr);
+    return energy_impl<double>(c, out, nullptr);
+}
+
+// sum |psi|^2 of the device field (no cell volume)
+static int raw_mass(gpss_ctx *c, double *out)
+{
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, 0) : diag_passes<double>(c, false, 0);
+    if (rc) return rc;
+    double h[4 * RQ_COUNT];
+    GPSS_TRY(read_sums(c, h));
+    if (!std::isfinite(h[RQ_MASS])) return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
+    *out = h[RQ_MASS];
+    return GPSS_OK;
+}
+
+int gpss_mass(gpss_ctx *c, double *out)
+{
+    if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_mass: null out") : GPSS_EINVAL;
+    double raw;
+    GPSS_TRY(raw_mass(c, &raw));
+    *out = times_cell(c, raw);
+    return GPSS_OK;
+}
+
+int gpss_norm(gpss_ctx *c, double *out)
+{
+    if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_norm: null out") : GPSS_EINVAL;
+    double raw;
+    GPSS_TRY(raw_mass(c, &raw));
+    // Fields.jl:172-180: sqrt(sum |psi|^2) * sqrt(dx dy [dz])
+    *out = std::sqrt(raw) * std::sqrt(cell_volume(c));
+    return GPSS_OK;
+}
+
+int gpss_normalize(gpss_ctx *c)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int zero = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, 1) : diag_passes<double>(c, false, 1);
+    if (rc) return rc;
+    rc = c->precision == GPSS_FP32 ? apply_scale<float>(c) : apply_scale<double>(c);
+    if (rc) return rc;
+    int st = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (st) return fail(c, GPSS_ENONFINITE, "normalize: non-finite or zero norm");
+    return GPSS_OK;
+}
+
+int gpss_ground_state(gpss_ctx *c, double dt, double tol, int64_t max_steps, int check_every,
+                      double *mu_out, int64_t *steps_out)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!(dt > 0) || !(tol > 0) || max_steps < 1 || check_every < 1)
+        return fail(c, GPSS_EINVAL, "ground_state: need dt > 0, tol > 0, max_steps >= 1, check_every >= 1");
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    double mu_prev = NAN, e[5] = {0, 0, 0, 0, 0};
+    int64_t done = 0;
+    GPSS_TRY(gpss_normalize(c));
+    while (done < max_steps) {
+        int64_t k = check_every;
+        if (k > max_steps - done) k = max_steps - done;
+        GPSS_TRY(gpss_step(c, (int)k, GPSS_STRANG, 1, dt, nullptr));
+        done += k;
+        GPSS_TRY(gpss_energy(c, e));
+        if (std::isfinite(mu_prev) && std::fabs(e[4] - mu_prev) < tol) break;
+        mu_prev = e[4];
+    }
+    if (mu_out) *mu_out = e[4];
+    if (steps_out) *steps_out = done;
+    return GPSS_OK;
+}
+
+int gpss_select_device(int device)
+{
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return device < 0 ? GPSS_EINVAL : GPSS_ECUDA;
+    }
+    return GPSS_OK;
+}
+
+int gpss_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+int gpss_sync(gpss_ctx *c)
+{
+    if (!c) return GPSS_EINVAL;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GPSS_OK;
+}
+
+int gpss_event_record(gpss_ctx *c, int slot)
+{
+    if (!c || slot < 0 || slot >= 8) return c ? fail(c, GPSS_EINVAL, "event slot must be 0..7") : GPSS_EINVAL;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaEventRecord(c->ev[slot], c->stream));
+    return GPSS_OK;
+}
+
+int gpss_event_elapsed(gpss_ctx *c, int a, int b, float *ms)
+{
+    if (!c || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return c ? fail(c, GPSS_EINVAL, "bad event slots") : GPSS_EINVAL;
+    CUDA_TRY(c, cudaEventSynchronize(c->ev[b]));
+    CUDA_TRY(c, cudaEventElapsedTime(ms, c->ev[a], c->ev[b]));
+    return GPSS_OK;
+}
+
+int64_t gpss_launch_count(const gpss_ctx *c) { return c ? c->launches : -1; }
+
+int64_t gpss_device_bytes(const gpss_ctx *c)
+{
+    if (!c) return -1;
+    return c->bytes;
+}
+
+int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double *ms_per_launch)
+{
+    if (!c || !ms_per_launch) return c ? fail(c, GPSS_EINVAL, "null argument") : GPSS_EINVAL;
+    if (axis < 0 || axis >= c->ndim || reps < 1 || (mode != 0 && mode != 1))
+        return fail(c, GPSS_EINVAL, "time_pass: bad axis/mode/reps");
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    auto run = [&](auto tag) -> int {
+        using T = decltype(tag);
+        PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
+        const void *ph;
+        GPSS_TRY(get_phase(c, axis, dt, 0, 1, &ph, &a.prow));
+        a.phase = (const vec2<T> *)ph;
+        if (mode == 1) {
+            a.nl_mode = NL_REAL;
+            a.V = c->have_V ? (const T *)c->V : nullptr;
+            a.nl_beta = c->beta;
+            a.nl_dt = dt;
+        }
+        GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));  // warm-up
+        CUDA_TRY(c, cudaEventRecord(c->ev[6], c->stream));
+        for (int i = 0; i < reps; i++) GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
+        CUDA_TRY(c, cudaEventRecord(c->ev[7], c->stream));
+        CUDA_TRY(c, cudaEventSynchronize(c->ev[7]));
+        float ms = 0.f;
+        CUDA_TRY(c, cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
+        *ms_per_launch = (double)ms / reps;
+        return GPSS_OK;
+    };
+    return c->precision == GPSS_FP32 ? run(0.0f) : run(0.0);
+}
+
+int gpss_host_alloc(void **ptr, int64_t bytes)
+{
+    if (!ptr || bytes <= 0) return GPSS_EINVAL;
+    cudaError_t e = cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        g_create_error = std::string("cudaHostAlloc: ") + cudaGetErrorString(e);
+        return GPSS_ENOMEM;
+    }
+    return GPSS_OK;
+}
+
+int gpss_host_free(void *ptr)
+{
+    if (!ptr) return GPSS_OK;
+    cudaError_t e = cudaFreeHost(ptr);
+    return e == cudaSuccess ? GPSS_OK : GPSS_ECUDA;
+}
+
+}  // extern "C"

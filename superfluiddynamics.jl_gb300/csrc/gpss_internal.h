@@ -1,0 +1,48 @@
+// gpss_internal.h -- declarations shared by the translation units of libgpss.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "pass_kernel.cuh"
+
+namespace gpss {
+
+// pass launchers (pass_f32.cu / pass_f64.cu)
+cudaError_t launch_pass_f32(int mode, bool xl, int n, const PassArgs<float> &a, int blocks,
+                            cudaStream_t s);
+cudaError_t launch_pass_f64(int mode, bool xl, int n, const PassArgs<double> &a, int blocks,
+                            cudaStream_t s);
+int pass_lines_per_cta_f32(int n, bool xl);
+int pass_lines_per_cta_f64(int n, bool xl);
+
+template <typename T> struct PassLauncher;
+template <> struct PassLauncher<float> {
+    static cudaError_t launch(int mode, bool xl, int n, const PassArgs<float> &a, int blocks,
+                              cudaStream_t s) { return launch_pass_f32(mode, xl, n, a, blocks, s); }
+    static int lines(int n, bool xl) { return pass_lines_per_cta_f32(n, xl); }
+};
+template <> struct PassLauncher<double> {
+    static cudaError_t launch(int mode, bool xl, int n, const PassArgs<double> &a, int blocks,
+                              cudaStream_t s) { return launch_pass_f64(mode, xl, n, a, blocks, s); }
+    static int lines(int n, bool xl) { return pass_lines_per_cta_f64(n, xl); }
+};
+
+// pointwise kernels (pointwise.cu)
+cudaError_t launch_f64_to_f32(const double *in, float *out, int64_t count, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const float *in, double *out, int64_t count, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mul_phase(vec2<T> *data, const vec2<T> *phase, int64_t prow, int axis,
+                             const int64_t *n, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t launch_nl(vec2<T> *psi, const T *V, double beta, double dt, int imag, int64_t total,
+                      cudaStream_t s);
+template <typename T>
+cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s);
+// sums partials[q * nblocks + b] over b for q < nq into out[q] (fixed order);
+// renorm != 0 also writes *scale_out = 1/sqrt(out[RQ_MASS] * dV) and sets
+// *status = 1 when the mass is not finite and positive.
+cudaError_t launch_finalize(const double *partials, int nblocks, int nq, double *out, int renorm,
+                            double dV, double *scale_out, int *status, cudaStream_t s);
+
+}  // namespace gpss

@@ -1,0 +1,84 @@
+// pass_dispatch.cuh -- host-side dispatch from run-time (mode, layout, n) to
+// the pass_kernel instantiation.  Included once per precision.
+#pragma once
+#include "pass_kernel.cuh"
+
+namespace gpss {
+
+template <typename T, int N, bool XL, int MODE>
+static cudaError_t launch_pass_inst(const PassArgs<T> &a, int blocks, cudaStream_t s)
+{
+    using S = PassShape<T, N, XL>;
+    auto k = pass_kernel<T, N, XL, MODE>;
+    if (S::SMEM_BYTES > 48 * 1024) {
+        // opt-in for more than 48 KB of dynamic shared memory (per device)
+        static bool done[64] = {false};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 0 || dev >= 64 || !done[dev]) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)S::SMEM_BYTES);
+            if (e != cudaSuccess) return e;
+            if (dev >= 0 && dev < 64) done[dev] = true;
+        }
+    }
+    k<<<blocks, S::THREADS, S::SMEM_BYTES, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, int N, bool XL>
+static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, cudaStream_t s)
+{
+    switch (mode) {
+    case MODE_FUSED: return launch_pass_inst<T, N, XL, MODE_FUSED>(a, blocks, s);
+    case MODE_FWD: return launch_pass_inst<T, N, XL, MODE_FWD>(a, blocks, s);
+    case MODE_INV: return launch_pass_inst<T, N, XL, MODE_INV>(a, blocks, s);
+    case MODE_DIAG: return launch_pass_inst<T, N, XL, MODE_DIAG>(a, blocks, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T, int N>
+static cudaError_t launch_pass_n(int mode, bool xl, const PassArgs<T> &a, int blocks, cudaStream_t s)
+{
+    return xl ? launch_pass_mode<T, N, true>(mode, a, blocks, s)
+              : launch_pass_mode<T, N, false>(mode, a, blocks, s);
+}
+
+template <typename T, int N> static int lines_per_cta_n(bool xl)
+{
+    return xl ? PassShape<T, N, true>::W : PassShape<T, N, false>::W;
+}
+
+#define GPSS_DEFINE_PASS_DISPATCH(T, SUFFIX)                                                   \
+    cudaError_t launch_pass_##SUFFIX(int mode, bool xl, int n, const PassArgs<T> &a,           \
+                                     int blocks, cudaStream_t s)                               \
+    {                                                                                          \
+        switch (n) {                                                                           \
+        case 2: return launch_pass_n<T, 2>(mode, xl, a, blocks, s);                            \
+        case 4: return launch_pass_n<T, 4>(mode, xl, a, blocks, s);                            \
+        case 8: return launch_pass_n<T, 8>(mode, xl, a, blocks, s);                            \
+        case 16: return launch_pass_n<T, 16>(mode, xl, a, blocks, s);                          \
+        case 32: return launch_pass_n<T, 32>(mode, xl, a, blocks, s);                          \
+        case 64: return launch_pass_n<T, 64>(mode, xl, a, blocks, s);                          \
+        case 128: return launch_pass_n<T, 128>(mode, xl, a, blocks, s);                        \
+        case 256: return launch_pass_n<T, 256>(mode, xl, a, blocks, s);                        \
+        default: return cudaErrorInvalidValue;                                                 \
+        }                                                                                      \
+    }                                                                                          \
+    int pass_lines_per_cta_##SUFFIX(int n, bool xl)                                            \
+    {                                                                                          \
+        switch (n) {                                                                           \
+        case 2: return lines_per_cta_n<T, 2>(xl);                                              \
+        case 4: return lines_per_cta_n<T, 4>(xl);                                              \
+        case 8: return lines_per_cta_n<T, 8>(xl);                                              \
+        case 16: return lines_per_cta_n<T, 16>(xl);                                            \
+        case 32: return lines_per_cta_n<T, 32>(xl);                                            \
+        case 64: return lines_per_cta_n<T, 64>(xl);                                            \
+        case 128: return lines_per_cta_n<T, 128>(xl);                                          \
+        case 256: return lines_per_cta_n<T, 256>(xl);                                          \
+        default: return 0;                                                                     \
+        }                                                                                      \
+    }
+
+}  // namespace gpss

@@ -1,0 +1,5 @@
+// FP32 instantiations of the directional pass kernels.
+#include "pass_dispatch.cuh"
+namespace gpss {
+GPSS_DEFINE_PASS_DISPATCH(float, f32)
+}

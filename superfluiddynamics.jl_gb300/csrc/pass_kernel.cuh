@@ -1,0 +1,360 @@
+// pass_kernel.cuh -- one directional split-step pass over every line of a
+// periodic 2D/3D field.
+//
+// A "line" is the set of cells that differ only in the coordinate of one
+// axis.  The reference moves each axis to the contiguous position with a
+// pencil transpose and calls a batched 1D FFT (mul_x!/mul_y!/mul_z!,
+// src/Discretization/Plans.jl:1132-1167), multiplies by the kinetic phase
+// (src/NumModels/GrossPitaevskii/splitting.jl:167, 172, 190, 195, 200) and
+// transforms back (ldiv_x!/..., Plans.jl:1207-1250).  Here one kernel reads
+// the lines in place (no transpose), so the whole FFT -> phase -> iFFT costs
+// one HBM read and one HBM write of the field.
+//
+// Line length n = N1 * N2 (N1 = min(n, 16)).  A line is processed by P = N2
+// threads, each holding N1 = 16 complex values in registers:
+//   stage A  load x[r + N2 j] (j < N1), forward DFT_N1, twiddle w_n^{r k1}
+//            -> shared memory slot (k1, r)
+//   stage B  thread k1 reads (k1, r) for r < N2, forward DFT_N2 gives
+//            X[k1 + N1 k2]; multiply by the phase; backward DFT_N2; twiddle
+//            conj(w_n^{r k1}) -> shared slot (k1, r)
+//   stage C  thread r reads (k1, r) for k1 < N1, backward DFT_N1 gives
+//            x[r + N2 j]; epilogue; store
+// The spectrum is never reordered: the forward transform ends and the
+// backward one starts in the same registers.  Lines of n <= 16 run entirely in
+// one thread.
+//
+// Two thread layouts:
+//   XL  (x axis, stride 1)    the P threads of a line are adjacent lanes, so
+//                             global accesses walk along the line;
+//   COL (y/z axes, strided)   W adjacent lanes hold W adjacent lines (adjacent
+//                             x columns), so each global access is a run of
+//                             W * sizeof(complex) >= 128 contiguous bytes.
+// Shared-memory layouts are chosen so every stage is bank-conflict free
+// (XL: one pad slot per N2-row plus N2 per line; COL: position-major).
+//
+// Modes:
+//   MODE_FUSED  FFT -> phase -> iFFT (+ optional NL epilogue, reductions)
+//   MODE_FWD    FFT only, writes the natural-order spectrum (plain form)
+//   MODE_INV    iFFT (with 1/n) from a natural-order spectrum (plain form)
+//   MODE_DIAG   FFT only, writes nothing, accumulates Parseval sums (energy)
+#pragma once
+#include <cstdint>
+#include "fft_core.cuh"
+#include "nl_phase.cuh"
+
+namespace gpss {
+
+enum { MODE_FUSED = 0, MODE_FWD = 1, MODE_INV = 2, MODE_DIAG = 3 };
+
+// reduction slots written by a pass (per-CTA partials, summed on the device)
+enum {
+    RQ_MASS = 0,   // sum |psi|^2
+    RQ_POT = 1,    // sum V |psi|^2
+    RQ_INT = 2,    // sum |psi|^4
+    RQ_KIN = 3,    // sum over lines of (1/n) sum_k xi_k^2 |X_k|^2
+    RQ_ROT = 4,    // sum over lines of c_line (1/n) sum_k xi_k |X_k|^2
+    RQ_COUNT = 5
+};
+enum { RED_POINT = 1, RED_KIN = 2 };
+enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
+
+template <typename T> struct PassArgs {
+    const vec2<T> *in;
+    vec2<T> *out;
+    const vec2<T> *tw;       // n entries, stage-A layout: tw[k1*N2 + r] = w_n^{r k1}
+    const vec2<T> *phase;    // phase[k + row*prow] (already includes 1/n in fused mode)
+    int64_t prow;            // 0: one table row for every line (held in shared memory)
+    int rowmod;              // row of line g is g % rowmod
+    int nlines;
+    int m0;                  // base(g) = (g % m0) * s0 + (g / m0) * s1
+    int64_t s0, s1, stride;  // stride between positions along the line
+    T inv_n;                 // MODE_INV scale (1/n)
+    // nonlinear epilogue (MODE_FUSED): psi <- exp(-i (V + beta|psi|^2) dt) psi
+    int nl_mode;
+    const T *V;              // nullable (zero potential)
+    double nl_beta, nl_dt;
+    // deferred renormalisation: multiply the input by *scale (nullable)
+    const double *scale;
+    // reductions
+    int red;                 // RED_POINT | RED_KIN
+    double *partials;        // [RQ_COUNT][gridDim.x]
+    double kmult;            // xi_k = kk * kmult, kk the signed wavenumber index
+    const double *coord;     // coordinate of each row (rotation energy), nullable
+};
+
+template <typename T> struct PassGeom {
+    static constexpr int THREADS = 256;
+};
+
+template <int N> struct Split {
+    static constexpr int N1 = N <= 16 ? N : 16;
+    static constexpr int N2 = N / N1;
+};
+
+template <typename T, int N, bool XL> struct PassShape {
+    static constexpr int N1 = Split<N>::N1;
+    static constexpr int N2 = Split<N>::N2;
+    static constexpr int P = N2;                       // threads per line
+    static constexpr int THREADS = PassGeom<T>::THREADS;
+    static constexpr int W = THREADS / P;              // lines per CTA
+    static constexpr int LS = N + N1 + N2;             // XL padded line stride (slots)
+    static constexpr int DATA = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
+    static constexpr int SMEM_SLOTS = DATA + 2 * N;    // + twiddle + phase tables
+    static constexpr size_t SMEM_BYTES = sizeof(vec2<T>) * SMEM_SLOTS;
+};
+
+// sum of `v` over the CTA, written by thread 0 into partials[q * gridDim.x + blockIdx.x]
+template <typename T, int THREADS>
+__device__ __forceinline__ void block_sum_store(T v, double *partials, int q, T *red_smem)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red_smem[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < THREADS / 32; i++) s += (double)red_smem[i];
+        partials[(size_t)q * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+template <typename T, int N, bool XL, int MODE>
+__global__ void __launch_bounds__(PassGeom<T>::THREADS)
+pass_kernel(const PassArgs<T> a)
+{
+    using V = vec2<T>;
+    using S = PassShape<T, N, XL>;
+    constexpr int N1 = S::N1, N2 = S::N2, P = S::P, W = S::W, LS = S::LS;
+    constexpr int THREADS = S::THREADS;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *sdata = reinterpret_cast<V *>(smem_raw);
+    V *stw = sdata + S::DATA;
+    V *sph = stw + N;
+
+    const int tid = threadIdx.x;
+    // tables into shared memory
+    for (int i = tid; i < N; i += THREADS) {
+        stw[i] = a.tw[i];
+        if (MODE == MODE_FUSED && a.prow == 0) sph[i] = a.phase[i];
+    }
+
+    const int w = XL ? tid / P : tid % W;
+    const int r = XL ? tid % P : tid / W;
+    const int g = blockIdx.x * W + w;
+    const bool valid = g < a.nlines;
+    const int gg = valid ? g : 0;
+    const int64_t base = (int64_t)(gg % a.m0) * a.s0 + (int64_t)(gg / a.m0) * a.s1;
+    const int row = gg % a.rowmod;
+    const int64_t st = a.stride;
+
+    auto sidx = [&](int q) -> int {
+        if constexpr (XL) return w * LS + q + q / N2;
+        else return q * W + w;
+    };
+
+    T scale = (T)1;
+    if (a.scale) scale = (T)(*a.scale);
+    const T kmult = (T)a.kmult;
+
+    // accumulators (precision of the field; the CTA totals are kept in FP64)
+    T acc_mass = 0, acc_pot = 0, acc_int = 0, acc_kin = 0, acc_rot = 0;
+
+    V v[N1];
+    if constexpr (MODE != MODE_INV) {
+#pragma unroll
+        for (int j = 0; j < N1; j++) {
+            v[j] = valid ? a.in[base + (int64_t)(r + N2 * j) * st] : mk<V>((T)0, (T)0);
+        }
+        if constexpr (MODE == MODE_DIAG) {
+            if (a.red & RED_POINT) {
+#pragma unroll
+                for (int j = 0; j < N1; j++) {
+                    T rho = v[j].x * v[j].x + v[j].y * v[j].y;
+                    acc_mass += rho;
+                    acc_int += rho * rho;
+                    if (a.V && valid) acc_pot += a.V[base + (int64_t)(r + N2 * j) * st] * rho;
+                }
+            }
+        }
+        dft<N1, -1>(v);
+    }
+    __syncthreads();  // tables ready
+
+    if constexpr (N2 == 1) {
+        // the whole line lives in this thread: v[k] = X[k]
+        if constexpr (MODE == MODE_FUSED) {
+            if (a.red & RED_KIN) {
+                T s2 = 0, s1 = 0;
+#pragma unroll
+                for (int k = 0; k < N1; k++) {
+                    const int kk = k < N / 2 ? k : k - N;
+                    const T xi = (T)kk * kmult;
+                    const T m2 = v[k].x * v[k].x + v[k].y * v[k].y;
+                    s2 += xi * xi * m2;
+                    s1 += xi * m2;
+                }
+                acc_kin += s2 * (T)(1.0 / N);
+                if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
+            }
+#pragma unroll
+            for (int k = 0; k < N1; k++) {
+                V ph = a.prow ? a.phase[k + row * a.prow] : sph[k];
+                v[k] = cmul(v[k], cscale(ph, scale));
+            }
+            dft<N1, +1>(v);
+        } else if constexpr (MODE == MODE_DIAG) {
+            if (a.red & RED_KIN) {
+                T s2 = 0, s1 = 0;
+#pragma unroll
+                for (int k = 0; k < N1; k++) {
+                    const int kk = k < N / 2 ? k : k - N;
+                    const T xi = (T)kk * kmult;
+                    const T m2 = v[k].x * v[k].x + v[k].y * v[k].y;
+                    s2 += xi * xi * m2;
+                    s1 += xi * m2;
+                }
+                acc_kin += s2 * (T)(1.0 / N);
+                if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
+            }
+        } else if constexpr (MODE == MODE_FWD) {
+            // spectrum out in natural order
+        } else {  // MODE_INV
+#pragma unroll
+            for (int j = 0; j < N1; j++)
+                v[j] = valid ? a.in[base + (int64_t)j * st] : mk<V>((T)0, (T)0);
+            dft<N1, +1>(v);
+#pragma unroll
+            for (int j = 0; j < N1; j++) v[j] = cscale(v[j], a.inv_n);
+        }
+    } else {
+        // ---- stage A store: (k1, r) <- v[k1] * w_n^{r k1}
+        if constexpr (MODE != MODE_INV) {
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) {
+                V t = k1 == 0 ? v[k1] : cmul(v[k1], stw[k1 * N2 + r]);
+                sdata[sidx(k1 * N2 + r)] = t;
+            }
+            __syncthreads();
+        }
+        // ---- stage B: items k1 = r + P*i
+        constexpr int NI = N1 / N2;
+#pragma unroll
+        for (int i = 0; i < NI; i++) {
+            const int k1 = r + P * i;
+            V u[N2];
+            if constexpr (MODE == MODE_INV) {
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++)
+                    u[k2] = valid ? a.in[base + (int64_t)(k1 + N1 * k2) * st] : mk<V>((T)0, (T)0);
+            } else {
+#pragma unroll
+                for (int rr = 0; rr < N2; rr++) u[rr] = sdata[sidx(k1 * N2 + rr)];
+                dft<N2, -1>(u);  // u[k2] = X[k1 + N1 k2]
+            }
+            if constexpr (MODE == MODE_FWD) {
+                if (valid) {
+#pragma unroll
+                    for (int k2 = 0; k2 < N2; k2++) a.out[base + (int64_t)(k1 + N1 * k2) * st] = u[k2];
+                }
+                continue;
+            }
+            if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
+                if (a.red & RED_KIN) {
+                    T s2 = 0, s1 = 0;
+#pragma unroll
+                    for (int k2 = 0; k2 < N2; k2++) {
+                        const int k = k1 + N1 * k2;
+                        const int kk = k < N / 2 ? k : k - N;
+                        const T xi = (T)kk * kmult;
+                        const T m2 = u[k2].x * u[k2].x + u[k2].y * u[k2].y;
+                        s2 += xi * xi * m2;
+                        s1 += xi * m2;
+                    }
+                    acc_kin += s2 * (T)(1.0 / N);
+                    if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
+                }
+            }
+            if constexpr (MODE == MODE_DIAG) continue;
+            if constexpr (MODE == MODE_FUSED) {
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++) {
+                    const int k = k1 + N1 * k2;
+                    V ph = a.prow ? a.phase[k + row * a.prow] : sph[k];
+                    u[k2] = cmul(u[k2], cscale(ph, scale));
+                }
+            }
+            dft<N2, +1>(u);  // u[rr] = Z[k1][rr]
+#pragma unroll
+            for (int rr = 0; rr < N2; rr++) {
+                V t = (k1 == 0 || rr == 0) ? u[rr] : cmulc(u[rr], stw[k1 * N2 + rr]);
+                sdata[sidx(k1 * N2 + rr)] = t;
+            }
+        }
+        if constexpr (MODE != MODE_FWD && MODE != MODE_DIAG) {
+            __syncthreads();
+            // ---- stage C
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) v[k1] = sdata[sidx(k1 * N2 + r)];
+            dft<N1, +1>(v);  // v[j] = x[r + N2 j] (times n unless folded)
+            if constexpr (MODE == MODE_INV) {
+#pragma unroll
+                for (int j = 0; j < N1; j++) v[j] = cscale(v[j], a.inv_n);
+            }
+        }
+    }
+
+    // ---- epilogue: positions r + N2 j
+    if constexpr (MODE == MODE_FUSED || MODE == MODE_INV) {
+        if constexpr (MODE == MODE_FUSED) {
+            if (a.nl_mode != NL_NONE) {
+                const NLConst<T> nlc(a.nl_beta, a.nl_dt);
+                const bool imag = a.nl_mode == NL_IMAG;
+#pragma unroll
+                for (int j = 0; j < N1; j++) {
+                    const T vv = (a.V && valid) ? a.V[base + (int64_t)(r + N2 * j) * st] : (T)0;
+                    v[j] = nl_apply(v[j], vv, nlc, imag);
+                }
+            }
+            if (a.red & RED_POINT) {
+#pragma unroll
+                for (int j = 0; j < N1; j++) {
+                    const T rho = v[j].x * v[j].x + v[j].y * v[j].y;
+                    acc_mass += rho;
+                    acc_int += rho * rho;
+                    if (a.V && valid) acc_pot += a.V[base + (int64_t)(r + N2 * j) * st] * rho;
+                }
+            }
+        }
+        if (valid) {
+#pragma unroll
+            for (int j = 0; j < N1; j++) a.out[base + (int64_t)(r + N2 * j) * st] = v[j];
+        }
+    } else if constexpr (MODE == MODE_FWD && N2 == 1) {
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < N1; k++) a.out[base + (int64_t)k * st] = v[k];
+        }
+    }
+
+    if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
+        if (a.red) {
+            __shared__ T red_smem[THREADS / 32];
+            if (!valid) { acc_mass = acc_pot = acc_int = acc_kin = acc_rot = 0; }
+            if (a.red & RED_POINT) {
+                block_sum_store<T, THREADS>(acc_mass, a.partials, RQ_MASS, red_smem);
+                block_sum_store<T, THREADS>(acc_pot, a.partials, RQ_POT, red_smem);
+                block_sum_store<T, THREADS>(acc_int, a.partials, RQ_INT, red_smem);
+            }
+            if (a.red & RED_KIN) {
+                block_sum_store<T, THREADS>(acc_kin, a.partials, RQ_KIN, red_smem);
+                block_sum_store<T, THREADS>(acc_rot, a.partials, RQ_ROT, red_smem);
+            }
+        }
+    }
+}
+
+}  // namespace gpss

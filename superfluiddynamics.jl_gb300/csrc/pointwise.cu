@@ -1,0 +1,150 @@
+// pointwise.cu -- element-wise kernels: precision conversion at the host
+// boundary, the plain-form phase multiply and nonlinear step, deferred
+// renormalisation, and the fixed-order finish of the CTA-partial reductions.
+#include "gpss_internal.h"
+
+namespace gpss {
+
+static int grid_for(int64_t count, int threads)
+{
+    int64_t b = (count + threads - 1) / threads;
+    const int64_t cap = 152 * 16;  // 16 CTAs of 256 threads per SM, grid-stride beyond
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+__global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ out, int64_t count)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+__global__ void k_f32_to_f64(const float *__restrict__ in, double *__restrict__ out, int64_t count)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+cudaError_t launch_f64_to_f32(const double *in, float *out, int64_t count, cudaStream_t s)
+{
+    k_f64_to_f32<<<grid_for(count, 256), 256, 0, s>>>(in, out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_f64(const float *in, double *out, int64_t count, cudaStream_t s)
+{
+    k_f32_to_f64<<<grid_for(count, 256), 256, 0, s>>>(in, out, count);
+    return cudaGetLastError();
+}
+
+// Plain form: psi_hat(k, row) *= phase[k + row * prow] on a natural-order
+// spectrum along `axis` (the broadcasts of splitting.jl:167/172/190/195/200).
+template <typename T>
+__global__ void k_mul_phase(vec2<T> *__restrict__ data, const vec2<T> *__restrict__ phase,
+                            int64_t prow, int axis, int64_t nx, int64_t ny, int64_t total)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t k, row;
+        if (axis == 0) { k = e % nx; row = (e / nx) % ny; }
+        else if (axis == 1) { k = (e / nx) % ny; row = e % nx; }
+        else { k = e / (nx * ny); row = 0; }
+        data[e] = cmul(phase[k + row * prow], data[e]);
+    }
+}
+
+template <typename T>
+cudaError_t launch_mul_phase(vec2<T> *data, const vec2<T> *phase, int64_t prow, int axis,
+                             const int64_t *n, int64_t total, cudaStream_t s)
+{
+    k_mul_phase<T><<<grid_for(total, 256), 256, 0, s>>>(data, phase, prow, axis, n[0], n[1], total);
+    return cudaGetLastError();
+}
+
+// Plain form: solveNL! (splitting.jl:205-209) as its own sweep.
+template <typename T>
+__global__ void k_nl(vec2<T> *__restrict__ psi, const T *__restrict__ V, double beta, double dt,
+                     int imag, int64_t total)
+{
+    const NLConst<T> c(beta, dt);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const T vv = V ? V[e] : (T)0;
+        psi[e] = nl_apply(psi[e], vv, c, imag != 0);
+    }
+}
+
+template <typename T>
+cudaError_t launch_nl(vec2<T> *psi, const T *V, double beta, double dt, int imag, int64_t total,
+                      cudaStream_t s)
+{
+    k_nl<T><<<grid_for(total, 256), 256, 0, s>>>(psi, V, beta, dt, imag, total);
+    return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void k_scale(vec2<T> *__restrict__ psi, const double *__restrict__ scale, int64_t total)
+{
+    const T s = (T)(*scale);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x)
+        psi[e] = cscale(psi[e], s);
+}
+
+template <typename T>
+cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s)
+{
+    k_scale<T><<<grid_for(total, 256), 256, 0, s>>>(psi, scale, total);
+    return cudaGetLastError();
+}
+
+__global__ void k_finalize(const double *__restrict__ partials, int nblocks, int nq,
+                           double *__restrict__ out, int renorm, double dV,
+                           double *__restrict__ scale_out, int *__restrict__ status)
+{
+    __shared__ double sh[256];
+    for (int q = 0; q < nq; q++) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(size_t)q * nblocks + b];
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[q] = sh[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && renorm) {
+        const double m = out[RQ_MASS];
+        if (!(m > 0.0) || !isfinite(m)) {
+            if (status) *status = 1;
+            *scale_out = 1.0;
+        } else {
+            *scale_out = 1.0 / (sqrt(m) * sqrt(dV));
+        }
+    }
+}
+
+cudaError_t launch_finalize(const double *partials, int nblocks, int nq, double *out, int renorm,
+                            double dV, double *scale_out, int *status, cudaStream_t s)
+{
+    k_finalize<<<1, 256, 0, s>>>(partials, nblocks, nq, out, renorm, dV, scale_out, status);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_mul_phase<float>(vec2<float> *, const vec2<float> *, int64_t, int,
+                                             const int64_t *, int64_t, cudaStream_t);
+template cudaError_t launch_mul_phase<double>(vec2<double> *, const vec2<double> *, int64_t, int,
+                                              const int64_t *, int64_t, cudaStream_t);
+template cudaError_t launch_nl<float>(vec2<float> *, const float *, double, double, int, int64_t,
+                                      cudaStream_t);
+template cudaError_t launch_nl<double>(vec2<double> *, const double *, double, double, int, int64_t,
+                                       cudaStream_t);
+template cudaError_t launch_scale<float>(vec2<float> *, const double *, int64_t, cudaStream_t);
+template cudaError_t launch_scale<double>(vec2<double> *, const double *, int64_t, cudaStream_t);
+
+}  // namespace gpss

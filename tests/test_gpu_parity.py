@@ -1,0 +1,303 @@
+"""Parity of the CUDA split-step path with the CPU oracle (FP64 restatement of
+src/NumModels/GrossPitaevskii/splitting.jl), through the library's public API.
+
+Tolerances (relative L2, ||a-b|| / ||b||, the metric of test/runtests.jl:1416):
+  FP64 forms  <= 1e-12   (the reference asserts 1e-10 for CuArray vs Array)
+  FP32 fused  <= 1e-5    (vs the FP64 oracle)
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import random_field, run_model
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    return built_lib
+
+
+# -------------------------------------------------- the reference's own case --
+@pytest.mark.parametrize("form", ["fused", "plain"])
+def test_reference_gpu_vs_cpu_split2(sfd, O, form):
+    """test/runtests.jl:1438-1454: 32^2 on [-6,6]^2, Gaussian*(1+0.1x),
+    normalised, beta=10, harmonic trap, dt=0.01, 20 steps of NumModelSplit2."""
+    g = sfd.Grid((32, 32), ((-6, 6), (-6, 6)))
+    f = sfd.Field(g)
+    X, Y = f.mesh()
+    f.phi = np.exp(-0.5 * (X ** 2 + Y ** 2)) * (1 + 0.1 * X)
+    sfd.normalize(f)
+    psi0 = f.phi.copy(order="F")
+    pot = sfd.PotentialQuadratic(f, gx=1.0, gy=1.0)
+    p = sfd.GrossPitaevskiiParameters(pot, coeffD=-0.5, beta=10.0, Omega=0.0)
+    n = sfd.NumModelSplit2(f, p, 0.01, 20, 20, precision="fp64", form=form)
+    for _ in range(20):
+        assert sfd.timeStep(n) == 2
+    got = f.phi.copy()
+    n.close()
+    ref = O.c_step(psi0, g.bounds, coeffD=-0.5, beta=10.0, V=pot.V, nsteps=20, dt=0.01)
+    assert O.rel_l2(got, ref) < TOL64
+
+
+# ------------------------------------------------------------ FP64 coverage --
+SHAPES = [
+    ((2, 4), 2), ((8, 8), 2), ((16, 32), 2), ((64, 16), 2), ((256, 8), 2), ((8, 256), 2),
+    ((128, 128), 2), ((256, 256), 2),
+    ((4, 8, 2), 3), ((32, 16, 8), 3), ((8, 16, 32), 3), ((64, 32, 16), 3), ((16, 16, 256), 3),
+    ((256, 16, 8), 3),
+]
+
+
+@pytest.mark.parametrize("shape,nd", SHAPES)
+def test_fp64_fused_shapes(sfd, O, shape, nd):
+    bounds = tuple((-3.0 - a, 4.0 + 0.5 * a) for a in range(nd))
+    psi0 = random_field(shape, seed=sum(shape))
+    V = O.quadratic_potential(shape, bounds, gammas=[1.0, 0.7, 1.3][:nd])
+    kw = dict(coeffD=-0.5, beta=3.0, V=V, dt=2e-3, nsteps=5)
+    got = run_model(sfd, shape, bounds, psi0, **kw)
+    ref = O.c_step(psi0, bounds, coeffD=-0.5, beta=3.0, V=V, nsteps=5, dt=2e-3)
+    assert O.rel_l2(got, ref) < TOL64
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("form", ["fused", "plain"])
+@pytest.mark.parametrize("shape", [(32, 64), (16, 32, 8)])
+def test_fp64_rotation(sfd, O, scheme, form, shape):
+    nd = len(shape)
+    bounds = tuple((-5.0, 5.0 + a) for a in range(nd))
+    psi0 = random_field(shape, seed=7)
+    V = O.quadratic_potential(shape, bounds)
+    got = run_model(sfd, shape, bounds, psi0, coeffD=-0.5, beta=20.0, omega=0.7, V=V, dt=5e-3,
+                    nsteps=6, scheme=scheme, form=form)
+    ref = O.c_step(psi0, bounds, coeffD=-0.5, beta=20.0, omega=0.7, V=V, nsteps=6, scheme=scheme,
+                   dt=5e-3)
+    assert O.rel_l2(got, ref) < TOL64
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("form", ["fused", "plain"])
+@pytest.mark.parametrize("shape", [(64, 32), (16, 8, 32)])
+def test_fp64_imaginary_time(sfd, O, scheme, form, shape):
+    nd = len(shape)
+    bounds = tuple((-6.0, 6.0) for _ in range(nd))
+    psi0 = random_field(shape, seed=3)
+    V = O.quadratic_potential(shape, bounds)
+    got = run_model(sfd, shape, bounds, psi0, coeffD=-0.5, beta=50.0, omega=0.3, V=V, dt=1e-2,
+                    nsteps=7, scheme=scheme, imag=True, form=form)
+    ref = O.c_step(psi0, bounds, coeffD=-0.5, beta=50.0, omega=0.3, V=V, nsteps=7, scheme=scheme,
+                   imag=True, dt=1e-2)
+    assert O.rel_l2(got, ref) < TOL64
+    dV = np.prod([(b[1] - b[0]) / n for n, b in zip(shape, bounds)])
+    assert abs(np.sum(np.abs(got) ** 2) * dV - 1.0) < 1e-12
+
+
+def test_merge_is_exact_reordering(sfd, O):
+    """Merging L(dt/2) L(dt/2) of consecutive steps (Omega = 0) only changes round-off."""
+    shape, bounds = (64, 32, 16), ((-4, 4), (-4, 4), (-2, 2))
+    psi0 = random_field(shape, seed=11)
+    V = O.quadratic_potential(shape, bounds)
+    a = run_model(sfd, shape, bounds, psi0, beta=30.0, V=V, dt=1e-3, nsteps=20, merge=True)
+    b = run_model(sfd, shape, bounds, psi0, beta=30.0, V=V, dt=1e-3, nsteps=20, merge=False)
+    c = run_model(sfd, shape, bounds, psi0, beta=30.0, V=V, dt=1e-3, nsteps=20, per_call=1)
+    ref = O.c_step(psi0, bounds, beta=30.0, V=V, nsteps=20, dt=1e-3)
+    for x in (a, b, c):
+        assert O.rel_l2(x, ref) < TOL64
+
+
+# --------------------------------------------------------- known answers --
+def test_linear_flow_is_exact(sfd, O):
+    """beta = V = Omega = 0: psi_hat(t) = exp(i coeffD k^2 t) psi_hat(0) exactly
+    (the split step is exact for the linear flow)."""
+    shape, bounds = (32, 16, 64), ((-np.pi, np.pi), (-2.0, 2.0), (0.0, 3.0))
+    psi0 = random_field(shape, seed=5)
+    t = 40 * 1e-2
+    got = run_model(sfd, shape, bounds, psi0, beta=0.0, dt=1e-2, nsteps=40)
+    F = np.fft.fftn(psi0)
+    for a, (n, b) in enumerate(zip(shape, bounds)):
+        xi = np.fft.fftfreq(n, (b[1] - b[0]) / n) * 2 * np.pi
+        s = [1] * 3
+        s[a] = n
+        F = F * np.exp(1j * (-0.5) * xi.reshape(s) ** 2 * t)
+    exact = np.fft.ifftn(F)
+    assert O.rel_l2(got, exact) < 1e-13
+
+
+def test_split_order_and_mass(sfd, O):
+    """test/runtests.jl:644-671 on the GPU: temporal order 1 (Lie) / 2 (Strang)
+    by step refinement, mass conserved to 1e-12."""
+    N, L, beta, T = 32, 2 * np.pi, 20.0, 0.2
+    bounds = ((-L, L), (-L, L))
+    g = sfd.Grid((N, N), bounds)
+    f = sfd.Field(g)
+    X, Y = f.mesh()
+    psi0 = np.asfortranarray((1 + 0.3 * np.cos(X) + 0.2 * np.sin(2 * Y)) * np.exp(1j * 0.5 * X))
+    psi0 = psi0 / O.c_norm(psi0, bounds)
+    for order, lo, hi, ns in ((1, 0.85, 1.15, (50, 100, 200)), (2, 1.85, 2.15, (25, 50, 100))):
+        runs = [run_model(sfd, (N, N), bounds, psi0, beta=beta, dt=T / k, nsteps=k, scheme=order)
+                for k in ns]
+        d = [np.sqrt(np.sum(np.abs(runs[i] - runs[i + 1]) ** 2) / np.sum(np.abs(runs[i + 1]) ** 2))
+             for i in range(2)]
+        assert lo < math.log2(d[0] / d[1]) < hi
+        masses = [np.sum(np.abs(r) ** 2) for r in runs]
+        assert max(abs(m - masses[0]) for m in masses) < 1e-12
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 1e-6)])
+def test_energy_matches_oracle(sfd, O, precision, tol):
+    for shape in ((64, 32), (32, 16, 8)):
+        nd = len(shape)
+        bounds = tuple((-5.0, 6.0) for _ in range(nd))
+        psi0 = random_field(shape, seed=21)
+        V = O.quadratic_potential(shape, bounds)
+        g = sfd.Grid(shape, bounds)
+        f = sfd.Field(g)
+        f.phi = psi0
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=-0.4, beta=7.0, Omega=0.6)
+        n = sfd.NumModelSplit2(f, p, 1e-3, 1, 1, precision=precision)
+        got = n.energies()
+        n.close()
+        ref = O.c_energy(psi0, bounds, coeffD=-0.4, beta=7.0, omega=0.6, V=V)
+        scale = max(abs(v) for v in ref)
+        for a, b in zip(got, ref):
+            assert abs(a - b) <= tol * scale
+
+
+def test_step_diagnostics_fused_equal_separate(sfd, O):
+    """The diagnostics fused into the final half step equal energy() after it."""
+    shape, bounds = (64, 64, 32), ((-5, 5), (-5, 5), (-3, 3))
+    psi0 = random_field(shape, seed=2)
+    V = O.quadratic_potential(shape, bounds)
+    g = sfd.Grid(shape, bounds)
+    f = sfd.Field(g)
+    f.phi = psi0
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=-0.5, beta=15.0)
+    n = sfd.NumModelSplit2(f, p, 1e-3, 10, 10, precision="fp64")
+    d = n.step(10, diag=True)
+    e = n.energies()
+    m = n.mass()
+    n.close()
+    assert abs(d["mass"] - m) <= 1e-13 * abs(m)
+    for a, b in zip(d["energy"], e):
+        assert abs(a - b) <= 1e-12 * max(abs(x) for x in e)
+
+
+# ------------------------------------------------------ benchmark configs --
+def test_cfg0_fp64_full(sfd, O, W):
+    """cfg0 at its full size: 128^2, g=500, trap, dt=1e-3, 1000 steps (FP64)."""
+    c = W.cfg0()
+    ref = O.c_step(c["psi"], c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"],
+                   nsteps=c["nsteps"], dt=c["dt"])
+    for form in ("fused", "plain"):
+        got = run_model(sfd, c["shape"], c["bounds"], c["psi"], coeffD=c["coeffD"], beta=c["beta"],
+                        V=c["V"], dt=c["dt"], nsteps=c["nsteps"], form=form, per_call=250)
+        assert O.rel_l2(got, ref) < TOL64
+        dV = (16.0 / 128) ** 2
+        assert abs(np.sum(np.abs(got) ** 2) * dV - 1.0) < 1e-12
+
+
+def test_cfg0_fp32(sfd, O, W):
+    c = W.cfg0()
+    ref = O.c_step(c["psi"], c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"],
+                   nsteps=c["nsteps"], dt=c["dt"])
+    got = run_model(sfd, c["shape"], c["bounds"], c["psi"], coeffD=c["coeffD"], beta=c["beta"],
+                    V=c["V"], dt=c["dt"], nsteps=c["nsteps"], precision="fp32")
+    assert O.rel_l2(got, ref) < TOL32
+
+
+def test_cfg1_fp32_128_vs_oracle(sfd, O, W):
+    """cfg1 physics at 128^3 (the oracle finishes in about a minute): FP32 fused
+    after 200 steps within 1e-5 of the FP64 oracle."""
+    c = W.cfg1(128)
+    ref = O.c_step(c["psi"], c["bounds"], coeffD=c["coeffD"], beta=c["beta"], nsteps=c["nsteps"],
+                   dt=c["dt"])
+    got = run_model(sfd, c["shape"], c["bounds"], c["psi"], coeffD=c["coeffD"], beta=c["beta"],
+                    dt=c["dt"], nsteps=c["nsteps"], precision="fp32")
+    assert O.rel_l2(got, ref) < TOL32
+
+
+def test_cfg1_fullsize_fp32_vs_fp64(sfd, O, W):
+    """cfg1 at 256^3: FP32 fused vs the FP64 plain kernels (pinned to the oracle
+    above) after 200 steps, plus mass and energy conservation in FP64 sums."""
+    c = W.cfg1(256)
+    res = {}
+    for prec, form in (("fp32", "fused"), ("fp64", "plain")):
+        g = sfd.Grid(c["shape"], c["bounds"])
+        f = sfd.Field(g)
+        f.phi = c["psi"]
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+        n = sfd.NumModelSplit2(f, p, c["dt"], c["nsteps"], c["nsteps"], precision=prec, form=form)
+        e0 = n.energies()
+        m0 = n.mass()
+        d = n.step(c["nsteps"], diag=True)
+        res[prec] = (f.phi.copy(order="F"), m0, e0, d)
+        n.close()
+    a, m0, e0, d = res["fp32"]
+    b = res["fp64"][0]
+    assert O.rel_l2(a, b) < TOL32
+    assert abs(d["mass"] - m0) / m0 < 1e-5
+    assert abs(d["energy"][3] - e0[3]) / abs(e0[3]) < 1e-3
+
+
+def test_cfg2_ground_state_small(sfd, O, W):
+    """Imaginary time (cfg2 physics at 32^3): FP32 stages with FP64 reductions
+    track the FP64 oracle; mu agrees."""
+    c = W.cfg2(32)
+    nsteps = 300
+    ref = O.c_step(c["psi"], c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"],
+                   nsteps=nsteps, dt=c["dt"], imag=True)
+    for prec, tol in (("fp64", TOL64), ("fp32", TOL32)):
+        got = run_model(sfd, c["shape"], c["bounds"], c["psi"], coeffD=c["coeffD"], beta=c["beta"],
+                        V=c["V"], dt=c["dt"], nsteps=nsteps, imag=True, precision=prec)
+        assert O.rel_l2(got, ref) < tol
+    mu_ref = O.c_energy(ref, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"])[4]
+    g = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(g)
+    f.phi = c["psi"]
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, c["V"]), coeffD=c["coeffD"], beta=c["beta"])
+    n = sfd.NumModelSplit2(f, p, c["dt"], nsteps, nsteps, precision="fp32")
+    n.step(nsteps, imag=True)
+    mu = n.energies()[4]
+    n.close()
+    assert abs(mu - mu_ref) / abs(mu_ref) < 1e-5
+
+
+# ----------------------------------------------------------------- errors --
+def test_nonfinite_is_reported(sfd):
+    g = sfd.Grid((16, 16), ((-1, 1), (-1, 1)))
+    f = sfd.Field(g)
+    a = np.ones((16, 16), dtype=complex)
+    a[3, 4] = np.nan
+    f.phi = a
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), beta=1.0)
+    n = sfd.NumModelSplit2(f, p, 1e-3, 1, 1)
+    with pytest.raises(sfd.GPSSError) as ei:
+        n.energies()
+    assert ei.value.code == -4
+    with pytest.raises(sfd.GPSSError):
+        n.step(2, imag=True)
+    n.close(download=False)
+
+
+# ------------------------------------------------------------ golden files --
+def _golden():
+    import os
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    return sorted(os.path.join(here, f) for f in os.listdir(here) if f.endswith(".npz"))
+
+
+@pytest.mark.parametrize("path", _golden(), ids=lambda p: p.split("/")[-1][:-4])
+@pytest.mark.parametrize("form", ["fused", "plain"])
+def test_golden_fixture(sfd, O, path, form):
+    z = np.load(path)
+    b = tuple(tuple(r) for r in z["bounds"])
+    V = z["V"] if z["has_V"] else None
+    got = run_model(sfd, z["psi0"].shape, b, z["psi0"], coeffD=float(z["coeffD"]), beta=float(z["beta"]),
+                    omega=float(z["omega"]), V=V, dt=float(z["dt"]), nsteps=int(z["nsteps"]),
+                    scheme=int(z["scheme"]), imag=bool(z["imag"]), form=form)
+    assert O.rel_l2(got, z["psi"]) < TOL64
