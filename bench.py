@@ -53,8 +53,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpss", choices=["gpss", "reference"])
     ap.add_argument("--n", type=int, default=CELLS_N, help="grid points per axis (default 256)")
+    ap.add_argument("--timesteps", type=int, default=TIMESTEPS_PER_STEP,
+                    help="time steps per bench step (default 200, the cfg1 run length)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
 
 
@@ -232,7 +235,7 @@ def run_gpss(args, rank, world, local):
     _lib.check(L.gpss_select_device(local))
     c = W.cfg1(args.n)
     cells = float(math.prod(c["shape"]))
-    nt = TIMESTEPS_PER_STEP
+    nt = args.timesteps
 
     grid = sfd.Grid(c["shape"], c["bounds"])
     f = sfd.Field(grid)
@@ -282,25 +285,29 @@ def run_gpss(args, rank, world, local):
 
     # ---- end to end through the public API with host buffers
     nbytes = int(cells) * 16
-    hbuf = ctypes.c_void_p()
-    _lib.check(L.gpss_host_alloc(ctypes.byref(hbuf), nbytes))
-    host = np.frombuffer((ctypes.c_char * nbytes).from_address(hbuf.value), dtype=np.complex128)
-    host[:] = c["psi"].reshape(-1, order="F")
-    hp = ctypes.cast(hbuf, ctypes.POINTER(ctypes.c_double))
-    e2e_steps = max(3, min(args.steps, 10))
-    ck(L.gpss_upload(h, hp))
-    ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
-    ck(L.gpss_download(h, hp))
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    e2e = None
+    e2e_steps = 0
+    if not args.no_e2e:
+        hbuf = ctypes.c_void_p()
+        _lib.check(L.gpss_host_alloc(ctypes.byref(hbuf), nbytes))
+        host = np.frombuffer((ctypes.c_char * nbytes).from_address(hbuf.value), dtype=np.complex128)
+        host[:] = c["psi"].reshape(-1, order="F")
+        hp = ctypes.cast(hbuf, ctypes.POINTER(ctypes.c_double))
+        e2e_steps = max(3, min(args.steps, 10))
         ck(L.gpss_upload(h, hp))
         ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
         ck(L.gpss_download(h, hp))
-    ck(L.gpss_sync(h))
-    e2e_s = dist.max(time.perf_counter() - t0)
-    e2e = world * cells * nt * e2e_steps / e2e_s / 1e6
-    _lib.check(L.gpss_host_free(hbuf))
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ck(L.gpss_upload(h, hp))
+            ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+            ck(L.gpss_download(h, hp))
+        ck(L.gpss_sync(h))
+        e2e_s = dist.max(time.perf_counter() - t0)
+        e2e = world * cells * nt * e2e_steps / e2e_s / 1e6
+        del host
+        _lib.check(L.gpss_host_free(hbuf))
     model.close(download=False)
 
     # ---- FP64 plain kernels on the same workload (fewer time steps)
@@ -350,8 +357,8 @@ def run_gpss(args, rank, world, local):
                    "l2": "inputs larger than L2 (134 MB field, 268 MB streamed per pass); no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gpu_launches": int(launches),
-        "e2e": {"value": e2e, "unit": "Mcell-steps/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
+        "e2e": None if e2e is None else {"value": e2e, "unit": "Mcell-steps/s", "h2d_bytes_per_step": nbytes,
+                                         "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "kernel": f"fused {dom} pass",
                      "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"

@@ -41,6 +41,10 @@ extern "C" {
                                  separate launches (no fusion, no merging) */
 #define GPSS_FLAG_NOMERGE 2   /* fused passes, but never merge the trailing and
                                  leading half kinetic steps of consecutive steps */
+#define GPSS_FLAG_NOMASSLOCK 4 /* FP32 real time: do not restore the mass of the
+                                 start of the call after each nonlinear stage */
+#define GPSS_FLAG_NOPIPE 8    /* fused passes without the asynchronous-copy pipeline
+                                 (same arithmetic, one tile per CTA) */
 
 /* split schemes of gpss_step */
 #define GPSS_LIE 1            /* NumModelSplit1: L(dt) N(dt) */

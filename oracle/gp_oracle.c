@@ -1,5 +1,5 @@
 /*
- * gp_oracle.c -- CPU restatement (FP64) of SuperfluidDynamics.jl's split-step
+ * gp_oracle.c -- CPU restatement of SuperfluidDynamics.jl's split-step
  * Gross-Pitaevskii path, used as the CHECKER of the CUDA library.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
@@ -27,6 +27,12 @@
  * reference at the round-off level, and parity is pinned by the reference's
  * analytic known-answer tests (test/runtests.jl:29-90, 644-671, 718-725).
  *
+ * Precision: the default build computes in FP64 (the reference's Float64).
+ * Built with -DOR_EXTENDED the same code computes in long double (80-bit on
+ * x86, 128-bit on Arm) and exports the entry points with an `_ext` suffix:
+ * a near-exact reference for measuring the round-off of FP64 implementations.
+ * Inputs, grid values and outputs stay doubles at the API either way.
+ *
  * Layout: column-major, x fastest (Julia Array order), complex interleaved
  * (re, im) doubles, exactly the memory of a Julia Array{ComplexF64}.
  *
@@ -42,11 +48,29 @@
 
 #define OR_TWO_PI 6.283185307179586 /* Float64(2pi), as Julia's 2pi literal */
 
-typedef struct { double re, im; } ocplx;
+#ifdef OR_EXTENDED
+typedef long double real;
+#define RCOS cosl
+#define RSIN sinl
+#define REXP expl
+#define RSQRT sqrtl
+#define RHALFPI 1.570796326794896619231321691639751442L
+#define OR_SYM(name) name##_ext
+#else
+typedef double real;
+#define RCOS cos
+#define RSIN sin
+#define REXP exp
+#define RSQRT sqrt
+#define RHALFPI 1.5707963267948966
+#define OR_SYM(name) name
+#endif
+
+typedef struct { real re, im; } ocplx;
 
 /* ---------------------------------------------------------------- grid --- */
 
-/* Julia Base.lerpi: t = j/d; (1-t)*a + t*b  (base/range.jl) */
+/* Julia Base.lerpi: t = j/d; (1-t)*a + t*b  (base/range.jl), in Float64 */
 static double lerpi(int64_t j, int64_t d, double a, double b)
 {
     double t = (double)j / (double)d;
@@ -56,7 +80,7 @@ static double lerpi(int64_t j, int64_t d, double a, double b)
 /* Grids.jl:78-84: x = LinRange(lo, hi, n+1)[1:end-1].  Indexing a LinRange
  * with a range builds LinRange(x[1], x[n], n), whose entries are lerps between
  * those two end points. */
-void or_grid_coords(int64_t n, double lo, double hi, double *x)
+static void grid_coords(int64_t n, double lo, double hi, double *x)
 {
     if (n <= 1) { x[0] = lo; return; }
     double first = lerpi(0, n, lo, hi);
@@ -65,8 +89,8 @@ void or_grid_coords(int64_t n, double lo, double hi, double *x)
 }
 
 /* Plans.jl:829-830: xi = fftfreq(n, 2pi/dx) (AbstractFFTs.Frequencies:
- * entry i is (i-1 - (i <= (n+1)>>1 ? 0 : n)) * (fs/n)). */
-void or_fftfreq(int64_t n, double dx, double *xi)
+ * entry i is (i-1 - (i <= (n+1)>>1 ? 0 : n)) * (fs/n)), in Float64. */
+static void fftfreq(int64_t n, double dx, double *xi)
 {
     double fs = OR_TWO_PI / dx;
     double mult = fs / (double)n;
@@ -77,23 +101,25 @@ void or_fftfreq(int64_t n, double dx, double *xi)
     }
 }
 
+void OR_SYM(or_grid_coords)(int64_t n, double lo, double hi, double *x) { grid_coords(n, lo, hi, x); }
+void OR_SYM(or_fftfreq)(int64_t n, double dx, double *xi) { fftfreq(n, dx, xi); }
+
 /* ----------------------------------------------------------------- FFT --- */
 
 /* (cos, sin) of 2 pi k / n, reduced to the first octant for accuracy and
  * exact symmetries. */
-static void unit_root(int64_t k, int64_t n, double *c, double *s)
+static void unit_root(int64_t k, int64_t n, real *c, real *s)
 {
     k %= n; if (k < 0) k += n;
-    /* quadrant */
-    int64_t q = (4 * k) / n;          /* 0..3 */
-    int64_t r4 = 4 * k - q * n;       /* remainder in units of 1/(4n) turns, [0,n) */
-    double cc, ss;
+    int64_t q = (4 * k) / n;          /* quadrant 0..3 */
+    int64_t r4 = 4 * k - q * n;       /* remainder, [0, n) in units of a quarter turn / n */
+    real cc, ss;
     if (2 * r4 <= n) {
-        double a = 0.5 * M_PI * (double)r4 / (double)n;
-        cc = cos(a); ss = sin(a);
+        real a = RHALFPI * (real)r4 / (real)n;
+        cc = RCOS(a); ss = RSIN(a);
     } else {
-        double a = 0.5 * M_PI * (double)(n - r4) / (double)n;
-        cc = sin(a); ss = cos(a);
+        real a = RHALFPI * (real)(n - r4) / (real)n;
+        cc = RSIN(a); ss = RCOS(a);
     }
     switch (q) {
     case 0: *c = cc;  *s = ss;  break;
@@ -118,7 +144,7 @@ static int plan_make(fftplan *p, int64_t n)
     p->tw = (ocplx *)malloc(sizeof(ocplx) * (size_t)(n > 0 ? n : 1));
     if (!p->tw) return -1;
     for (int64_t k = 0; k < n; k++) {
-        double c, s;
+        real c, s;
         unit_root(k, n, &c, &s);
         p->tw[k].re = c;
         p->tw[k].im = -s;
@@ -136,10 +162,10 @@ static void fft_line(const fftplan *p, ocplx *a, ocplx *tmp, int sign)
     if (n == 1) return;
     if (!p->pow2) { /* direct O(n^2) DFT for sizes that are not powers of two */
         for (int64_t k = 0; k < n; k++) {
-            double sr = 0.0, si = 0.0;
+            real sr = 0, si = 0;
             for (int64_t j = 0; j < n; j++) {
                 int64_t m = (j * k) % n;
-                double wr = p->tw[m].re, wi = sign < 0 ? p->tw[m].im : -p->tw[m].im;
+                real wr = p->tw[m].re, wi = sign < 0 ? p->tw[m].im : -p->tw[m].im;
                 sr += a[j].re * wr - a[j].im * wi;
                 si += a[j].re * wi + a[j].im * wr;
             }
@@ -161,11 +187,11 @@ static void fft_line(const fftplan *p, ocplx *a, ocplx *tmp, int sign)
         int64_t half = len >> 1, step = n / len;
         for (int64_t i = 0; i < n; i += len) {
             for (int64_t k = 0; k < half; k++) {
-                double wr = p->tw[k * step].re;
-                double wi = sign < 0 ? p->tw[k * step].im : -p->tw[k * step].im;
+                real wr = p->tw[k * step].re;
+                real wi = sign < 0 ? p->tw[k * step].im : -p->tw[k * step].im;
                 ocplx u = a[i + k], v = a[i + k + half];
-                double tr = v.re * wr - v.im * wi;
-                double ti = v.re * wi + v.im * wr;
+                real tr = v.re * wr - v.im * wi;
+                real ti = v.re * wi + v.im * wr;
                 a[i + k].re = u.re + tr; a[i + k].im = u.im + ti;
                 a[i + k + half].re = u.re - tr; a[i + k + half].im = u.im - ti;
             }
@@ -179,10 +205,10 @@ static void fft_line(const fftplan *p, ocplx *a, ocplx *tmp, int sign)
 typedef struct {
     int ndim;
     int64_t n[3];
-    double lo[3], hi[3], L[3], d[3];
+    double lo[3], hi[3], L[3], d[3];   /* Float64 grid description */
     int64_t total;
-    double *coord[3];
-    double *xi[3];
+    double *coord[3];                  /* node positions (Float64) */
+    double *xi[3];                     /* wavenumbers (Float64) */
     fftplan plan[3];
 } ogrid;
 
@@ -212,32 +238,32 @@ static int grid_make(ogrid *g, int ndim, const int64_t *n, const double *lo, con
         g->coord[a] = (double *)malloc(sizeof(double) * (size_t)g->n[a]);
         g->xi[a] = (double *)malloc(sizeof(double) * (size_t)g->n[a]);
         if (!g->coord[a] || !g->xi[a]) { grid_free(g); return -1; }
-        or_grid_coords(g->n[a], g->lo[a], g->hi[a], g->coord[a]);
-        or_fftfreq(g->n[a], g->d[a], g->xi[a]);
+        grid_coords(g->n[a], g->lo[a], g->hi[a], g->coord[a]);
+        fftfreq(g->n[a], g->d[a], g->xi[a]);
         if (a < ndim && plan_make(&g->plan[a], g->n[a])) { grid_free(g); return -1; }
     }
     return 0;
 }
 
-static double cell_volume(const ogrid *g)
+static real cell_volume(const ogrid *g)
 {
-    double v = 1.0;
-    for (int a = 0; a < g->ndim; a++) v *= g->d[a];
+    real v = 1;
+    for (int a = 0; a < g->ndim; a++) v *= (real)g->d[a];
     return v;
 }
 
 /* x * dx * dy [* dz], left to right as Julia evaluates `s * Δx * Δy * Δz` */
-static double times_cell(const ogrid *g, double x)
+static real times_cell(const ogrid *g, real x)
 {
-    for (int a = 0; a < g->ndim; a++) x *= g->d[a];
+    for (int a = 0; a < g->ndim; a++) x *= (real)g->d[a];
     return x;
 }
 
 /* Julia's sum is pairwise; so is this one (block of 1024 leaves). */
-static double pairwise_sum(const double *v, int64_t n)
+static real pairwise_sum(const real *v, int64_t n)
 {
     if (n <= 1024) {
-        double s = 0.0;
+        real s = 0;
         for (int64_t i = 0; i < n; i++) s += v[i];
         return s;
     }
@@ -245,59 +271,86 @@ static double pairwise_sum(const double *v, int64_t n)
     return pairwise_sum(v, h) + pairwise_sum(v + h, n - h);
 }
 
+/* double (re, im) pairs <-> internal complex */
+static ocplx *load_field(const double *psi, int64_t N)
+{
+    ocplx *p = (ocplx *)malloc(sizeof(ocplx) * (size_t)N);
+    if (!p) return NULL;
+    for (int64_t i = 0; i < N; i++) { p[i].re = (real)psi[2 * i]; p[i].im = (real)psi[2 * i + 1]; }
+    return p;
+}
+
+static void store_field(const ocplx *p, double *psi, int64_t N)
+{
+    for (int64_t i = 0; i < N; i++) { psi[2 * i] = (double)p[i].re; psi[2 * i + 1] = (double)p[i].im; }
+}
+
+static real *load_real(const double *v, int64_t N)
+{
+    if (!v) return NULL;
+    real *r = (real *)malloc(sizeof(real) * (size_t)N);
+    if (!r) return NULL;
+    for (int64_t i = 0; i < N; i++) r[i] = (real)v[i];
+    return r;
+}
+
 /* --------------------------------------------------- directional passes -- */
 
-/* For each line along `axis`: FFT, multiply by a per-(line, k) factor, iFFT.
- * mode selects the factor (all of splitting.jl:167/172/190/195/200):
+static int64_t line_base(const ogrid *g, int axis, int64_t l)
+{
+    int64_t nx = g->n[0], ny = g->n[1];
+    if (axis == 0) return l * nx;
+    if (axis == 1) return (l % nx) + (l / nx) * nx * ny;
+    return l;
+}
+
+static int64_t line_stride(const ogrid *g, int axis)
+{
+    return axis == 0 ? 1 : (axis == 1 ? g->n[0] : g->n[0] * g->n[1]);
+}
+
+/* coordinate of line l that enters the rotation term of `axis`:
+ * the y node for x lines, the x node for y lines */
+static real line_coord(const ogrid *g, int axis, int64_t l)
+{
+    if (axis == 0 && g->ndim >= 2) return (real)g->coord[1][l % g->n[1]];
+    if (axis == 1) return (real)g->coord[0][l % g->n[0]];
+    return 0;
+}
+
+/* For each line along `axis`: FFT, multiply, iFFT (splitting.jl:164-201):
  *   real time   exp(i (cD xi^2 - Om y xi) dtl)   (x)
  *               exp(i (cD xi^2 + Om x xi) dtl)   (y)
  *               exp(i  cD xi^2 dtl)              (z)
  *   imag time   the same with t -> -i tau: exp((cD xi^2 -/+ Om c xi) dtl).
  */
-static void kinetic_axis(const ogrid *g, ocplx *psi, int axis, double cD, double Om,
-                         double dtl, int imag)
+static void kinetic_axis(const ogrid *g, ocplx *psi, int axis, real cD, real Om, real dtl, int imag)
 {
     int64_t n = g->n[axis];
-    int64_t nx = g->n[0], ny = g->n[1], nz = g->n[2];
-    int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : nx * ny);
+    int64_t stride = line_stride(g, axis);
     int64_t nlines = g->total / n;
     const double *xi = g->xi[axis];
-    double inv_n = 1.0 / (double)n;
-    (void)nz;
+    real inv_n = (real)1 / (real)n;
 #pragma omp parallel
     {
         ocplx *line = (ocplx *)malloc(sizeof(ocplx) * (size_t)n);
         ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)n);
 #pragma omp for schedule(static)
         for (int64_t l = 0; l < nlines; l++) {
-            int64_t base, other;
-            if (axis == 0) {          /* lines indexed by (j, k) */
-                base = l * nx;
-                other = l % ny;       /* y index */
-            } else if (axis == 1) {   /* lines indexed by (i, k) */
-                int64_t i = l % nx, k = l / nx;
-                base = i + k * nx * ny;
-                other = i;            /* x index */
-            } else {
-                base = l;
-                other = 0;
-            }
+            int64_t base = line_base(g, axis, l);
+            real c = line_coord(g, axis, l);
             for (int64_t p = 0; p < n; p++) line[p] = psi[base + p * stride];
             fft_line(&g->plan[axis], line, tmp, -1);
-            /* coordinate of this line that enters the rotation term */
-            double c = 0.0;
-            if (axis == 0 && g->ndim >= 2) c = g->coord[1][other];
-            else if (axis == 1) c = g->coord[0][other];
             for (int64_t k = 0; k < n; k++) {
-                double xk = xi[k], ph;
+                real xk = (real)xi[k], ph;
                 /* Julia: coeffD * xi^2 -/+ Om * c * xi  (xi^2 == xi*xi) */
                 if (axis == 0) ph = cD * (xk * xk) - Om * c * xk;
                 else if (axis == 1) ph = cD * (xk * xk) + Om * c * xk;
                 else ph = cD * (xk * xk);
-                double fr, fi;
-                if (!imag) { double t = ph * dtl; fr = cos(t); fi = sin(t); }
-                else { fr = exp(ph * dtl); fi = 0.0; }
-                double ar = line[k].re, ai = line[k].im;
+                real fr, fi;
+                if (!imag) { real t = ph * dtl; fr = RCOS(t); fi = RSIN(t); }
+                else { fr = REXP(ph * dtl); fi = 0; }
+                real ar = line[k].re, ai = line[k].im;
                 line[k].re = fr * ar - fi * ai;
                 line[k].im = fr * ai + fi * ar;
             }
@@ -312,85 +365,87 @@ static void kinetic_axis(const ogrid *g, ocplx *psi, int axis, double cD, double
 }
 
 /* splitting.jl:156-203 solveLapRot!: x, then y, then z. */
-static void solve_lap_rot(const ogrid *g, ocplx *psi, double cD, double Om, double dtl, int imag)
+static void solve_lap_rot(const ogrid *g, ocplx *psi, real cD, real Om, real dtl, int imag)
 {
     for (int a = 0; a < g->ndim; a++) kinetic_axis(g, psi, a, cD, Om, dtl, imag);
 }
 
 /* splitting.jl:205-209 solveNL!: psi <- exp(-i (V + beta |psi|^2) dtl) psi;
  * imaginary time: psi <- exp(-(V + beta |psi|^2) dtl) psi. */
-static void solve_nl(const ogrid *g, ocplx *psi, const double *V, double beta, double dtl, int imag)
+static void solve_nl(const ogrid *g, ocplx *psi, const real *V, real beta, real dtl, int imag)
 {
     int64_t N = g->total;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < N; i++) {
-        double ar = psi[i].re, ai = psi[i].im;
-        double rho = ar * ar + ai * ai;                 /* abs2 */
-        double r = (V ? V[i] : 0.0) + beta * rho;
-        double fr, fi;
-        if (!imag) { double t = -r * dtl; fr = cos(t); fi = sin(t); }
-        else { fr = exp(-r * dtl); fi = 0.0; }
+        real ar = psi[i].re, ai = psi[i].im;
+        real rho = ar * ar + ai * ai;                   /* abs2 */
+        real r = (V ? V[i] : 0) + beta * rho;
+        real fr, fi;
+        if (!imag) { real t = -r * dtl; fr = RCOS(t); fi = RSIN(t); }
+        else { fr = REXP(-r * dtl); fi = 0; }
         psi[i].re = fr * ar - fi * ai;
         psi[i].im = fr * ai + fi * ar;
     }
 }
 
-static double sum_abs2(const ogrid *g, const ocplx *psi)
+static real sum_abs2(const ogrid *g, const ocplx *psi)
 {
     int64_t N = g->total;
-    double *tmp = (double *)malloc(sizeof(double) * (size_t)N);
+    real *tmp = (real *)malloc(sizeof(real) * (size_t)N);
     if (!tmp) return NAN;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < N; i++) tmp[i] = psi[i].re * psi[i].re + psi[i].im * psi[i].im;
-    double s = pairwise_sum(tmp, N);
+    real s = pairwise_sum(tmp, N);
     free(tmp);
     return s;
 }
 
 /* Fields.jl:172-180 */
-static double field_norm(const ogrid *g, const ocplx *psi)
+static real field_norm(const ogrid *g, const ocplx *psi)
 {
-    return sqrt(sum_abs2(g, psi)) * sqrt(cell_volume(g));
+    return RSQRT(sum_abs2(g, psi)) * RSQRT(cell_volume(g));
 }
 
 /* ------------------------------------------------------------ public API -- */
 
-double or_norm(int ndim, const int64_t *n, const double *lo, const double *hi, const double *psi)
+double OR_SYM(or_norm)(int ndim, const int64_t *n, const double *lo, const double *hi, const double *psi)
 {
     ogrid g;
     if (grid_make(&g, ndim, n, lo, hi)) return NAN;
-    double r = field_norm(&g, (const ocplx *)psi);
+    ocplx *p = load_field(psi, g.total);
+    double r = p ? (double)field_norm(&g, p) : NAN;
+    free(p);
     grid_free(&g);
     return r;
 }
 
 /* Batched 1D FFT along one axis (unnormalised forward, or backward*1/n when
  * inverse != 0) -- Plans.jl mul_x!/ldiv_x! etc. without the pencil moves. */
-int or_fft_axis(int ndim, const int64_t *n, double *psi, int axis, int inverse)
+int OR_SYM(or_fft_axis)(int ndim, const int64_t *n, double *psi, int axis, int inverse)
 {
     ogrid g;
     const double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
     if (grid_make(&g, ndim, n, lo, hi)) return -1;
     if (axis < 0 || axis >= ndim) { grid_free(&g); return -1; }
-    int64_t len = g.n[axis], nx = g.n[0], ny = g.n[1];
-    int64_t stride = axis == 0 ? 1 : (axis == 1 ? nx : nx * ny);
-    int64_t nlines = g.total / len;
-    ocplx *p = (ocplx *)psi;
+    int64_t len = g.n[axis], stride = line_stride(&g, axis), nlines = g.total / len;
+    ocplx *p = load_field(psi, g.total);
     ocplx *line = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
     ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
-    for (int64_t l = 0; l < nlines; l++) {
-        int64_t base = axis == 0 ? l * nx : (axis == 1 ? (l % nx) + (l / nx) * nx * ny : l);
+    int rc = (p && line && tmp) ? 0 : -1;
+    for (int64_t l = 0; rc == 0 && l < nlines; l++) {
+        int64_t base = line_base(&g, axis, l);
         for (int64_t q = 0; q < len; q++) line[q] = p[base + q * stride];
         fft_line(&g.plan[axis], line, tmp, inverse ? +1 : -1);
-        double s = inverse ? 1.0 / (double)len : 1.0;
+        real s = inverse ? (real)1 / (real)len : (real)1;
         for (int64_t q = 0; q < len; q++) {
             p[base + q * stride].re = line[q].re * s;
             p[base + q * stride].im = line[q].im * s;
         }
     }
-    free(line); free(tmp);
+    if (rc == 0) store_field(p, psi, g.total);
+    free(p); free(line); free(tmp);
     grid_free(&g);
-    return 0;
+    return rc;
 }
 
 /*
@@ -399,31 +454,35 @@ int or_fft_axis(int ndim, const int64_t *n, double *psi, int axis, int inverse)
  * imag != 0: imaginary time with unit-mass renormalisation after each step.
  * V may be NULL (PotentialZero).  nthreads <= 0 keeps the OpenMP default.
  */
-int or_step(int ndim, const int64_t *n, const double *lo, const double *hi,
-            double cD, double beta, double Om, const double *V, double *psi,
-            int nsteps, int scheme, int imag, double dt, int nthreads)
+int OR_SYM(or_step)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                    double cD, double beta, double Om, const double *V, double *psi,
+                    int nsteps, int scheme, int imag, double dt, int nthreads)
 {
     ogrid g;
     if (scheme != 1 && scheme != 2) return -1;
     if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    ocplx *p = load_field(psi, g.total);
+    real *Vr = load_real(V, g.total);
+    if (!p || (V && !Vr)) { free(p); free(Vr); grid_free(&g); return -1; }
 #ifdef _OPENMP
     int saved = omp_get_max_threads();
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
-    ocplx *p = (ocplx *)psi;
+    /* Julia: n.Δt * 0.5 is a Float64 product, then used as the step */
+    const real rdt = (real)dt, half = (real)(dt * 0.5);
     for (int s = 0; s < nsteps; s++) {
         if (scheme == 2) {
-            solve_lap_rot(&g, p, cD, Om, dt * 0.5, imag);
-            solve_nl(&g, p, V, beta, dt, imag);
-            solve_lap_rot(&g, p, cD, Om, dt * 0.5, imag);
+            solve_lap_rot(&g, p, (real)cD, (real)Om, half, imag);
+            solve_nl(&g, p, Vr, (real)beta, rdt, imag);
+            solve_lap_rot(&g, p, (real)cD, (real)Om, half, imag);
         } else {
-            solve_lap_rot(&g, p, cD, Om, dt, imag);
-            solve_nl(&g, p, V, beta, dt, imag);
+            solve_lap_rot(&g, p, (real)cD, (real)Om, rdt, imag);
+            solve_nl(&g, p, Vr, (real)beta, rdt, imag);
         }
         if (imag) {                       /* normalize!, Fields.jl:196-200 */
-            double nrm = field_norm(&g, p);
+            real nrm = field_norm(&g, p);
             int64_t N = g.total;
 #pragma omp parallel for schedule(static)
             for (int64_t i = 0; i < N; i++) { p[i].re /= nrm; p[i].im /= nrm; }
@@ -432,6 +491,8 @@ int or_step(int ndim, const int64_t *n, const double *lo, const double *hi,
 #ifdef _OPENMP
     omp_set_num_threads(saved);
 #endif
+    store_field(p, psi, g.total);
+    free(p); free(Vr);
     grid_free(&g);
     return 0;
 }
@@ -440,22 +501,13 @@ int or_step(int ndim, const int64_t *n, const double *lo, const double *hi,
  * Spectral derivatives of GradientRotField (derivatives.jl:27-56 for 2D,
  * 90-126 for 3D): d[axis] = iFFT(i xi FFT psi), dd = iFFT(-xi^2 FFT psi),
  * rx = iFFT_x(i y xi_x FFT_x psi), ry = iFFT_y(-i x xi_y FFT_y psi).
- * Outputs may be NULL.  Each non-NULL output holds total complex entries.
+ * Inputs/outputs are internal-precision fields; NULL outputs are skipped.
  */
-int or_derivatives(int ndim, const int64_t *n, const double *lo, const double *hi,
-                   const double *psi, double *dx, double *dy, double *dz,
-                   double *ddx, double *ddy, double *ddz, double *rx, double *ry)
+static void derivatives(const ogrid *g, const ocplx *p, ocplx **d1, ocplx **d2, ocplx **rr)
 {
-    ogrid g;
-    if (grid_make(&g, ndim, n, lo, hi)) return -1;
-    double *d1[3] = {dx, dy, dz}, *d2[3] = {ddx, ddy, ddz}, *rr[3] = {rx, ry, NULL};
-    const ocplx *p = (const ocplx *)psi;
-    int64_t nx = g.n[0], ny = g.n[1];
-    for (int a = 0; a < ndim; a++) {
-        int64_t len = g.n[a];
-        int64_t stride = a == 0 ? 1 : (a == 1 ? nx : nx * ny);
-        int64_t nlines = g.total / len;
-        double inv_n = 1.0 / (double)len;
+    for (int a = 0; a < g->ndim; a++) {
+        int64_t len = g->n[a], stride = line_stride(g, a), nlines = g->total / len;
+        real inv_n = (real)1 / (real)len;
 #pragma omp parallel
         {
             ocplx *hat = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
@@ -463,17 +515,15 @@ int or_derivatives(int ndim, const int64_t *n, const double *lo, const double *h
             ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
 #pragma omp for schedule(static)
             for (int64_t l = 0; l < nlines; l++) {
-                int64_t base = a == 0 ? l * nx : (a == 1 ? (l % nx) + (l / nx) * nx * ny : l);
-                double c = 0.0;
-                if (a == 0 && ndim >= 2) c = g.coord[1][l % ny];
-                if (a == 1) c = g.coord[0][l % nx];
+                int64_t base = line_base(g, a, l);
+                real c = line_coord(g, a, l);
                 for (int64_t q = 0; q < len; q++) hat[q] = p[base + q * stride];
-                fft_line(&g.plan[a], hat, tmp, -1);
+                fft_line(&g->plan[a], hat, tmp, -1);
                 for (int kind = 0; kind < 3; kind++) {
-                    double *out = kind == 0 ? d1[a] : (kind == 1 ? d2[a] : rr[a]);
-                    if (!out) continue;
+                    ocplx *o = kind == 0 ? d1[a] : (kind == 1 ? d2[a] : rr[a]);
+                    if (!o) continue;
                     for (int64_t k = 0; k < len; k++) {
-                        double xi = g.xi[a][k], hr = hat[k].re, hi_ = hat[k].im;
+                        real xi = (real)g->xi[a][k], hr = hat[k].re, hi_ = hat[k].im;
                         if (kind == 0) {        /* i xi hat */
                             line[k].re = -xi * hi_; line[k].im = xi * hr;
                         } else if (kind == 1) { /* -xi^2 hat */
@@ -484,8 +534,7 @@ int or_derivatives(int ndim, const int64_t *n, const double *lo, const double *h
                             line[k].re = (c * xi) * hi_; line[k].im = -(c * xi) * hr;
                         }
                     }
-                    fft_line(&g.plan[a], line, tmp, +1);
-                    ocplx *o = (ocplx *)out;
+                    fft_line(&g->plan[a], line, tmp, +1);
                     for (int64_t q = 0; q < len; q++) {
                         o[base + q * stride].re = line[q].re * inv_n;
                         o[base + q * stride].im = line[q].im * inv_n;
@@ -495,8 +544,33 @@ int or_derivatives(int ndim, const int64_t *n, const double *lo, const double *h
             free(hat); free(line); free(tmp);
         }
     }
+}
+
+int OR_SYM(or_derivatives)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                           const double *psi, double *dx, double *dy, double *dz,
+                           double *ddx, double *ddy, double *ddz, double *rx, double *ry)
+{
+    ogrid g;
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    double *outs[8] = {dx, dy, dz, ddx, ddy, ddz, rx, ry};
+    ocplx *in[8] = {0};
+    ocplx *p = load_field(psi, g.total);
+    int rc = p ? 0 : -1;
+    for (int i = 0; i < 8 && rc == 0; i++) {
+        if (!outs[i]) continue;
+        in[i] = (ocplx *)calloc((size_t)g.total, sizeof(ocplx));
+        if (!in[i]) rc = -1;
+    }
+    if (rc == 0) {
+        ocplx *d1[3] = {in[0], in[1], in[2]}, *d2[3] = {in[3], in[4], in[5]}, *rr[3] = {in[6], in[7], NULL};
+        derivatives(&g, p, d1, d2, rr);
+        for (int i = 0; i < 8; i++)
+            if (outs[i]) store_field(in[i], outs[i], g.total);
+    }
+    for (int i = 0; i < 8; i++) free(in[i]);
+    free(p);
     grid_free(&g);
-    return 0;
+    return rc;
 }
 
 /*
@@ -508,68 +582,69 @@ int or_derivatives(int ndim, const int64_t *n, const double *lo, const double *h
  *   out[4] = mu      = -E_Omega + E_Delta + 2 E_beta  (GrossPitaevskii.jl:79;
  *                      the 3D method computes no mu, the same formula is used)
  */
-int or_energy(int ndim, const int64_t *n, const double *lo, const double *hi,
-              double cD, double beta, double Om, const double *V, const double *psi,
-              double *out)
+int OR_SYM(or_energy)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                      double cD, double beta, double Om, const double *V, const double *psi,
+                      double *out)
 {
     ogrid g;
     if (grid_make(&g, ndim, n, lo, hi)) return -1;
     int64_t N = g.total;
-    double *d[3] = {NULL, NULL, NULL}, *rx = NULL, *ry = NULL, *tmp = NULL;
+    ocplx *d[3] = {NULL, NULL, NULL}, *rx = NULL, *ry = NULL;
+    real *tmp = NULL, *Vr = NULL;
+    ocplx *p = load_field(psi, N);
     int rc = -1;
+    if (!p) goto done;
     for (int a = 0; a < ndim; a++) {
-        d[a] = (double *)malloc(sizeof(double) * 2 * (size_t)N);
+        d[a] = (ocplx *)calloc((size_t)N, sizeof(ocplx));
         if (!d[a]) goto done;
     }
-    rx = (double *)calloc(2 * (size_t)N, sizeof(double));
-    ry = (double *)calloc(2 * (size_t)N, sizeof(double));
-    tmp = (double *)malloc(sizeof(double) * (size_t)N);
-    if (!rx || !ry || !tmp) goto done;
-    if (or_derivatives(ndim, n, lo, hi, psi, d[0], ndim > 1 ? d[1] : NULL, ndim > 2 ? d[2] : NULL,
-                       NULL, NULL, NULL, rx, ndim > 1 ? ry : NULL))
-        goto done;
-    const ocplx *p = (const ocplx *)psi;
-    double grad = 0.0;
+    rx = (ocplx *)calloc((size_t)N, sizeof(ocplx));
+    ry = (ocplx *)calloc((size_t)N, sizeof(ocplx));
+    tmp = (real *)malloc(sizeof(real) * (size_t)N);
+    Vr = load_real(V, N);
+    if (!rx || !ry || !tmp || (V && !Vr)) goto done;
+    {
+        ocplx *d2[3] = {NULL, NULL, NULL}, *rr[3] = {rx, ndim > 1 ? ry : NULL, NULL};
+        derivatives(&g, p, d, d2, rr);
+    }
+    real grad = 0;
     for (int a = 0; a < ndim; a++) {
-        const ocplx *da = (const ocplx *)d[a];
-        for (int64_t i = 0; i < N; i++) tmp[i] = da[i].re * da[i].re + da[i].im * da[i].im;
+        for (int64_t i = 0; i < N; i++) tmp[i] = d[a][i].re * d[a][i].re + d[a][i].im * d[a][i].im;
         grad += pairwise_sum(tmp, N);
     }
-    const ocplx *X = (const ocplx *)rx, *Y = (const ocplx *)ry;
     for (int64_t i = 0; i < N; i++) {
         /* real(im * conj(psi) * (Om * (rx + ry))) */
-        double sr = Om * (X[i].re + Y[i].re), si = Om * (X[i].im + Y[i].im);
-        double cr = p[i].re, ci = -p[i].im;                 /* conj(psi) */
-        double pr = cr * sr - ci * si, pi_ = cr * si + ci * sr;
+        real sr = (real)Om * (rx[i].re + ry[i].re), si = (real)Om * (rx[i].im + ry[i].im);
+        real cr = p[i].re, ci = -p[i].im;                  /* conj(psi) */
+        real pi_ = cr * si + ci * sr;
         tmp[i] = -pi_;                                       /* real(i * z) = -imag(z) */
-        (void)pr;
     }
-    double eom = times_cell(&g, pairwise_sum(tmp, N));
+    real eom = times_cell(&g, pairwise_sum(tmp, N));
     for (int64_t i = 0; i < N; i++) {
-        double r = p[i].re * p[i].re + p[i].im * p[i].im;
-        tmp[i] = (V ? V[i] : 0.0) * r;
+        real r = p[i].re * p[i].re + p[i].im * p[i].im;
+        tmp[i] = (Vr ? Vr[i] : 0) * r;
     }
-    double epot = pairwise_sum(tmp, N);
-    double edel = times_cell(&g, -cD * grad + epot);
+    real epot = pairwise_sum(tmp, N);
+    real edel = times_cell(&g, -(real)cD * grad + epot);
     for (int64_t i = 0; i < N; i++) {
-        double r = p[i].re * p[i].re + p[i].im * p[i].im;
-        tmp[i] = (0.5 * beta) * (r * r);
+        real r = p[i].re * p[i].re + p[i].im * p[i].im;
+        tmp[i] = ((real)0.5 * (real)beta) * (r * r);
     }
-    double ebeta = times_cell(&g, pairwise_sum(tmp, N));
-    out[0] = eom;
-    out[1] = edel;
-    out[2] = ebeta;
-    out[3] = -eom + edel + ebeta;
-    out[4] = -eom + edel + ebeta * 2.0;
+    real ebeta = times_cell(&g, pairwise_sum(tmp, N));
+    out[0] = (double)eom;
+    out[1] = (double)edel;
+    out[2] = (double)ebeta;
+    out[3] = (double)(-eom + edel + ebeta);
+    out[4] = (double)(-eom + edel + ebeta * 2);
     rc = 0;
 done:
     for (int a = 0; a < 3; a++) free(d[a]);
-    free(rx); free(ry); free(tmp);
+    free(rx); free(ry); free(tmp); free(Vr); free(p);
     grid_free(&g);
     return rc;
 }
 
-int or_max_threads(void)
+int OR_SYM(or_max_threads)(void)
 {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -23,37 +23,60 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libgporacle.so")
+_EXT_PATH = os.path.join(_HERE, "_build", "libgporacle_ext.so")
 _lib = None
+_ext = None
 
 _i64p = ctypes.POINTER(ctypes.c_int64)
 _f64p = ctypes.POINTER(ctypes.c_double)
 
 
 def build(force: bool = False) -> str:
-    """Compile gp_oracle.c with oracle/Makefile; returns the library path."""
-    if force or not os.path.exists(_LIB_PATH):
+    """Compile gp_oracle.c (FP64 and extended builds) with oracle/Makefile."""
+    if force or not (os.path.exists(_LIB_PATH) and os.path.exists(_EXT_PATH)):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
 
-def lib():
-    global _lib
+class _Bound:
+    """The or_* entry points of one build (suffix '' or '_ext')."""
+
+    def __init__(self, path, suffix):
+        L = ctypes.CDLL(path)
+        g = lambda nm: getattr(L, nm + suffix)
+        self.or_grid_coords = g("or_grid_coords")
+        self.or_grid_coords.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, _f64p]
+        self.or_fftfreq = g("or_fftfreq")
+        self.or_fftfreq.argtypes = [ctypes.c_int64, ctypes.c_double, _f64p]
+        self.or_norm = g("or_norm")
+        self.or_norm.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p]
+        self.or_norm.restype = ctypes.c_double
+        self.or_fft_axis = g("or_fft_axis")
+        self.or_fft_axis.argtypes = [ctypes.c_int, _i64p, _f64p, ctypes.c_int, ctypes.c_int]
+        self.or_step = g("or_step")
+        self.or_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        self.or_derivatives = g("or_derivatives")
+        self.or_derivatives.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p] + [_f64p] * 8
+        self.or_energy = g("or_energy")
+        self.or_energy.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, _f64p, _f64p, _f64p]
+        self.or_max_threads = g("or_max_threads")
+        self.or_max_threads.restype = ctypes.c_int
+
+
+def lib(extended: bool = False):
+    """FP64 oracle, or (extended=True) the long-double build of the same code."""
+    global _lib, _ext
+    if extended:
+        if _ext is None:
+            build()
+            _ext = _Bound(_EXT_PATH, "_ext")
+        return _ext
     if _lib is None:
         build()
-        L = ctypes.CDLL(_LIB_PATH)
-        L.or_grid_coords.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, _f64p]
-        L.or_fftfreq.argtypes = [ctypes.c_int64, ctypes.c_double, _f64p]
-        L.or_norm.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p]
-        L.or_norm.restype = ctypes.c_double
-        L.or_fft_axis.argtypes = [ctypes.c_int, _i64p, _f64p, ctypes.c_int, ctypes.c_int]
-        L.or_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
-                              ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
-                              ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
-        L.or_derivatives.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p] + [_f64p] * 8
-        L.or_energy.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
-                                ctypes.c_double, ctypes.c_double, _f64p, _f64p, _f64p]
-        L.or_max_threads.restype = ctypes.c_int
-        _lib = L
+        _lib = _Bound(_LIB_PATH, "")
     return _lib
 
 
@@ -123,12 +146,17 @@ def c_fft_axis(psi, axis: int, inverse: bool = False):
 
 
 def c_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, scheme=2,
-           imag=False, dt=1e-3, nthreads=0):
-    """nsteps of NumModelSplit2 (scheme=2) or NumModelSplit1 (scheme=1); returns a new array."""
-    out = _field(psi).copy(order="F")
+           imag=False, dt=1e-3, nthreads=0, extended=False, inplace=False):
+    """nsteps of NumModelSplit2 (scheme=2) or NumModelSplit1 (scheme=1).  Returns a
+    new array (or steps `psi` itself when inplace=True and it is an F-ordered
+    complex128 array).  extended=True runs the long-double build."""
+    if inplace and isinstance(psi, np.ndarray) and psi.dtype == np.complex128 and psi.flags.f_contiguous:
+        out = psi
+    else:
+        out = _field(psi).copy(order="F")
     nd, n, lo, hi = _geom(out.shape, bounds)
     Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
-    rc = lib().or_step(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
+    rc = lib(extended).or_step(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
                        _p(Vp), _p(out), int(nsteps), int(scheme),
                        1 if imag else 0, float(dt), int(nthreads))
     if rc != 0:
@@ -156,13 +184,13 @@ def c_derivatives(psi, bounds):
     return outs
 
 
-def c_energy(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None):
+def c_energy(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, extended=False):
     """energy(n) of GrossPitaevskii.jl:61-136 -> (E_Omega, E_Delta, E_beta, E, mu)."""
     psi = _field(psi)
     nd, n, lo, hi = _geom(psi.shape, bounds)
     out = np.zeros(5, dtype=np.float64)
     Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
-    rc = lib().or_energy(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
+    rc = lib(extended).or_energy(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
                          _p(Vp), _p(psi), _p(out))
     assert rc == 0
     return tuple(float(v) for v in out)

@@ -25,6 +25,8 @@ GPSS_FP64 = 64
 GPSS_FP32 = 32
 GPSS_FLAG_PLAIN = 1
 GPSS_FLAG_NOMERGE = 2
+GPSS_FLAG_NOMASSLOCK = 4
+GPSS_FLAG_NOPIPE = 8
 GPSS_LIE = 1
 GPSS_STRANG = 2
 

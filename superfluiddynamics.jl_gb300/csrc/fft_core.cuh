@@ -44,38 +44,71 @@ template <int DIR, typename V> __device__ __forceinline__ V mul_i(V a)
     return mk<V>(-a.y, a.x);
 }
 
+// Constants of the 16-point DFT as double-word pairs (hi + lo): cos(pi/8),
+// sin(pi/8), sqrt(1/2).  Multiplying by hi and adding the product with lo
+// leaves only the random rounding of the arithmetic; a rounded constant alone
+// would add the same relative error to the same frequency at every pass, an
+// error that a split-step run accumulates over thousands of passes.
+template <typename T> struct DftConst;
+template <> struct DftConst<float> {
+    static constexpr float C1h = 0.9238795042037964f, C1l = 2.830748968563057e-08f;
+    static constexpr float S1h = 0.3826834261417389f, S1l = 6.2233507236442165e-09f;
+    static constexpr float Hh = 0.7071067690849304f, Hl = 1.2101617485882343e-08f;
+};
+template <> struct DftConst<double> {
+    static constexpr double C1h = 0.9238795325112867, C1l = 1.7645047084336677e-17;
+    static constexpr double S1h = 0.3826834323650898, S1l = -1.0050772696461588e-17;
+    static constexpr double Hh = 0.7071067811865476, Hl = -4.833646656726457e-17;
+};
+
+// a * (bh + bl), b given as a double-word complex constant
+template <typename V> __device__ __forceinline__ V cmul2(V a, V bh, V bl)
+{
+    using T = decltype(V::x);
+    const T lx = fma(a.x, bl.x, -a.y * bl.y);
+    const T ly = fma(a.x, bl.y, a.y * bl.x);
+    return mk<V>(fma(a.x, bh.x, fma(-a.y, bh.y, lx)), fma(a.x, bh.y, fma(a.y, bh.x, ly)));
+}
+// a * conj(bh + bl)
+template <typename V> __device__ __forceinline__ V cmulc2(V a, V bh, V bl)
+{
+    using T = decltype(V::x);
+    const T lx = fma(a.x, bl.x, a.y * bl.y);
+    const T ly = fma(a.y, bl.x, -a.x * bl.y);
+    return mk<V>(fma(a.x, bh.x, fma(a.y, bh.y, lx)), fma(a.y, bh.x, fma(-a.x, bh.y, ly)));
+}
+// t * (hi + lo) for a real double-word constant
+template <typename T> __device__ __forceinline__ T rmul2(T t, T hi, T lo) { return fma(t, hi, t * lo); }
+
 // Multiply by w16^m = exp(DIR * 2 pi i m / 16) for a compile-time m.
 template <int M, int DIR, typename V> __device__ __forceinline__ V mul_w16(V a)
 {
     using T = decltype(V::x);
+    using K = DftConst<T>;
     constexpr int m = ((M % 16) + 16) % 16;
-    const T C1 = (T)0.92387953251128675613;  // cos(pi/8)
-    const T S1 = (T)0.38268343236508977173;  // sin(pi/8)
-    const T H = (T)0.70710678118654752440;   // sqrt(1/2)
-    // angle = DIR * 2 pi m / 16 ; value = cos(angle) + i sin(angle)
     if constexpr (m == 0) return a;
     else if constexpr (m == 4) return mul_i<DIR>(a);
     else if constexpr (m == 8) return mk<V>(-a.x, -a.y);
     else if constexpr (m == 12) return mul_i<-DIR>(a);
     else if constexpr (m % 2 == 0) {
-        // odd multiple of pi/4: (+-1 +- i)/sqrt2
+        // odd multiple of pi/4: value = (sc + i ss) / sqrt2 with sc, ss = +-1
         constexpr int q = m / 2;  // 1, 3, 5, 7
-        const T cr = (q == 1 || q == 7) ? H : -H;
-        const T si = (q == 1 || q == 3) ? (T)DIR * H : -(T)DIR * H;
-        return mk<V>((a.x * cr - a.y * si), (a.x * si + a.y * cr));
+        constexpr int sc = (q == 1 || q == 7) ? 1 : -1;
+        constexpr int ss = ((q == 1 || q == 3) ? 1 : -1) * DIR;
+        // (a.x + i a.y)(sc + i ss) = (sc a.x - ss a.y) + i (ss a.x + sc a.y)
+        const T re = sc * a.x - ss * a.y;
+        const T im = ss * a.x + sc * a.y;
+        return mk<V>(rmul2(re, K::Hh, K::Hl), rmul2(im, K::Hh, K::Hl));
     } else {
-        // odd multiple of pi/8
-        T cr, sr;  // cos, sin of 2 pi m/16 (positive orientation)
-        if constexpr (m == 1) { cr = C1; sr = S1; }
-        else if constexpr (m == 3) { cr = S1; sr = C1; }
-        else if constexpr (m == 5) { cr = -S1; sr = C1; }
-        else if constexpr (m == 7) { cr = -C1; sr = S1; }
-        else if constexpr (m == 9) { cr = -C1; sr = -S1; }
-        else if constexpr (m == 11) { cr = -S1; sr = -C1; }
-        else if constexpr (m == 13) { cr = S1; sr = -C1; }
-        else { cr = C1; sr = -S1; }  // 15
-        const T si = (T)DIR * sr;
-        return mk<V>(a.x * cr - a.y * si, a.x * si + a.y * cr);
+        // odd multiple of pi/8: cos/sin are +-C1 / +-S1
+        constexpr int ci = (m == 1 || m == 15) ? 1 : (m == 3 || m == 13) ? 2 : (m == 5 || m == 11) ? -2 : -1;
+        constexpr int si = (m == 1 || m == 7) ? 2 : (m == 3 || m == 5) ? 1 : (m == 9 || m == 15) ? -2 : -1;
+        // ci/si: +-1 selects C1, +-2 selects S1 (cos(2 pi m/16), sin(2 pi m/16))
+        const T crh = (ci == 1 || ci == -1) ? (T)(ci > 0 ? K::C1h : -K::C1h) : (T)(ci > 0 ? K::S1h : -K::S1h);
+        const T crl = (ci == 1 || ci == -1) ? (T)(ci > 0 ? K::C1l : -K::C1l) : (T)(ci > 0 ? K::S1l : -K::S1l);
+        const T srh = (si == 2 || si == -2) ? (T)(si > 0 ? K::S1h : -K::S1h) : (T)(si > 0 ? K::C1h : -K::C1h);
+        const T srl = (si == 2 || si == -2) ? (T)(si > 0 ? K::S1l : -K::S1l) : (T)(si > 0 ? K::C1l : -K::C1l);
+        return cmul2(a, mk<V>(crh, (T)DIR * srh), mk<V>(crl, (T)DIR * srl));
     }
 }
 

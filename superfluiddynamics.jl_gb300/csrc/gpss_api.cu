@@ -42,9 +42,10 @@ struct gpss_ctx {
     std::vector<double> coord[3];
     double *partials = nullptr;
     int max_blocks = 0;
-    double *sums = nullptr;   // [4][RQ_COUNT]
+    double *sums = nullptr;   // [4][RQ_COUNT]: slots 0..2 per axis, slot 3 diagnostics
     double *scale = nullptr;  // [1]
     int *status = nullptr;    // [1]
+    unsigned int *counter = nullptr;  // arrival counter of the in-kernel reduction finish
     std::vector<PhaseEntry> phases;
     cudaEvent_t ev[8] = {};
     int64_t launches = 0;
@@ -91,21 +92,24 @@ static int dev_alloc(gpss_ctx *c, void **p, size_t bytes)
     return GPSS_OK;
 }
 
-// (cos, sin) of 2 pi k / n, reduced to the first octant so that the
-// symmetric values are exact.
-static void unit_root(int64_t k, int64_t n, double *cs, double *sn)
+typedef long double ldouble;
+static const ldouble kHalfPiL = 1.570796326794896619231321691639751442L;
+
+// (cos, sin) of 2 pi k / n in long double, reduced to the first octant so
+// that the symmetric values are exact.
+static void unit_root(int64_t k, int64_t n, ldouble *cs, ldouble *sn)
 {
     k %= n;
     if (k < 0) k += n;
     int64_t q = (4 * k) / n;
     int64_t r4 = 4 * k - q * n;
-    double cc, ss;
+    ldouble cc, ss;
     if (2 * r4 <= n) {
-        double a = 0.5 * M_PI * (double)r4 / (double)n;
-        cc = std::cos(a); ss = std::sin(a);
+        ldouble a = kHalfPiL * (ldouble)r4 / (ldouble)n;
+        cc = cosl(a); ss = sinl(a);
     } else {
-        double a = 0.5 * M_PI * (double)(n - r4) / (double)n;
-        cc = std::sin(a); ss = std::cos(a);
+        ldouble a = kHalfPiL * (ldouble)(n - r4) / (ldouble)n;
+        cc = sinl(a); ss = cosl(a);
     }
     switch (q) {
     case 0: *cs = cc; *sn = ss; break;
@@ -142,18 +146,40 @@ static double xi_of(const gpss_ctx *c, int axis, int64_t k)
 static size_t cplx_bytes(const gpss_ctx *c) { return c->precision == GPSS_FP32 ? 8 : 16; }
 static size_t real_bytes(const gpss_ctx *c) { return c->precision == GPSS_FP32 ? 4 : 8; }
 
-// upload n doubles as T
-static int upload_table(gpss_ctx *c, void **dev, const std::vector<double> &h)
+// Upload complex values v[0..cnt) (cnt = rows * n, row-major) as double-word
+// pairs in the field precision: per row hi[n] then lo[n], hi + lo = v.
+static int upload_dw(gpss_ctx *c, void **dev, const std::vector<ldouble> &re, const std::vector<ldouble> &im,
+                     int64_t rows, int64_t n)
 {
-    size_t cnt = h.size();
-    GPSS_TRY(dev_alloc(c, dev, cnt * real_bytes(c)));
+    std::vector<double> h((size_t)(4 * n * rows));  // re/im pairs of hi and lo as doubles
+    std::vector<ldouble> lo_re(re.size()), lo_im(im.size());
     if (c->precision == GPSS_FP32) {
-        std::vector<float> f(cnt);
-        for (size_t i = 0; i < cnt; i++) f[i] = (float)h[i];
-        CUDA_TRY(c, cudaMemcpy(*dev, f.data(), cnt * 4, cudaMemcpyHostToDevice));
-    } else {
-        CUDA_TRY(c, cudaMemcpy(*dev, h.data(), cnt * 8, cudaMemcpyHostToDevice));
+        std::vector<float> f((size_t)(4 * n * rows));
+        for (int64_t r = 0; r < rows; r++)
+            for (int64_t k = 0; k < n; k++) {
+                const size_t i = (size_t)(r * n + k);
+                const float hr = (float)re[i], hi = (float)im[i];
+                const float lr = (float)(re[i] - (ldouble)hr), li = (float)(im[i] - (ldouble)hi);
+                f[(size_t)(2 * (r * 2 * n + k))] = hr;
+                f[(size_t)(2 * (r * 2 * n + k) + 1)] = hi;
+                f[(size_t)(2 * (r * 2 * n + n + k))] = lr;
+                f[(size_t)(2 * (r * 2 * n + n + k) + 1)] = li;
+            }
+        GPSS_TRY(dev_alloc(c, dev, f.size() * 4));
+        CUDA_TRY(c, cudaMemcpy(*dev, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+        return GPSS_OK;
     }
+    for (int64_t r = 0; r < rows; r++)
+        for (int64_t k = 0; k < n; k++) {
+            const size_t i = (size_t)(r * n + k);
+            const double hr = (double)re[i], hi = (double)im[i];
+            h[(size_t)(2 * (r * 2 * n + k))] = hr;
+            h[(size_t)(2 * (r * 2 * n + k) + 1)] = hi;
+            h[(size_t)(2 * (r * 2 * n + n + k))] = (double)(re[i] - (ldouble)hr);
+            h[(size_t)(2 * (r * 2 * n + n + k) + 1)] = (double)(im[i] - (ldouble)hi);
+        }
+    GPSS_TRY(dev_alloc(c, dev, h.size() * 8));
+    CUDA_TRY(c, cudaMemcpy(*dev, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
     return GPSS_OK;
 }
 
@@ -175,25 +201,27 @@ static int get_phase(gpss_ctx *c, int axis, double dtl, int imag, int fused, con
     const int64_t n = c->n[axis];
     const bool rot = c->omega != 0.0 && axis < 2 && c->ndim >= 2;
     const int64_t rows = rot ? (axis == 0 ? c->n[1] : c->n[0]) : 1;
-    std::vector<double> h((size_t)(2 * n * rows));
-    const double inv_n = fused ? 1.0 / (double)n : 1.0;
+    std::vector<ldouble> re((size_t)(n * rows)), im((size_t)(n * rows));
+    const ldouble inv_n = fused ? 1.0L / (ldouble)n : 1.0L;
     for (int64_t r = 0; r < rows; r++) {
         const double cr = rot ? (axis == 0 ? c->coord[1][(size_t)r] : c->coord[0][(size_t)r]) : 0.0;
         for (int64_t k = 0; k < n; k++) {
+            // the phase argument is the reference's Float64 expression; its
+            // exponential is evaluated in long double and kept as hi + lo
             const double xk = xi_of(c, axis, k);
             double ph;
             if (axis == 0) ph = c->cD * (xk * xk) - c->omega * cr * xk;
             else if (axis == 1) ph = c->cD * (xk * xk) + c->omega * cr * xk;
             else ph = c->cD * (xk * xk);
-            double fr, fi;
-            if (!imag) { double t = ph * dtl; fr = std::cos(t); fi = std::sin(t); }
-            else { fr = std::exp(ph * dtl); fi = 0.0; }
-            h[(size_t)(2 * (k + r * n))] = fr * inv_n;
-            h[(size_t)(2 * (k + r * n) + 1)] = fi * inv_n;
+            ldouble fr, fi;
+            if (!imag) { const ldouble t = (ldouble)(ph * dtl); fr = cosl(t); fi = sinl(t); }
+            else { fr = expl((ldouble)(ph * dtl)); fi = 0.0L; }
+            re[(size_t)(r * n + k)] = fr * inv_n;
+            im[(size_t)(r * n + k)] = fi * inv_n;
         }
     }
-    PhaseEntry e{axis, imag, fused, dtl, c->cD, c->omega, nullptr, rot ? n : 0};
-    GPSS_TRY(upload_table(c, &e.dev, h));
+    PhaseEntry e{axis, imag, fused, dtl, c->cD, c->omega, nullptr, rot ? 2 * n : 0};
+    GPSS_TRY(upload_dw(c, &e.dev, re, im, rows, n));
     if (c->phases.size() > 64) {  // bounded cache: drop the oldest
         cudaStreamSynchronize(c->stream);
         cudaFree(c->phases.front().dev);
@@ -238,8 +266,30 @@ template <typename T> static int blocks_for(gpss_ctx *c, int axis)
     return (int)((nl + W - 1) / W);
 }
 
+// Can the pipelined kernel run this fused pass?  Its tiles are 4096/n whole
+// lines; y tiles must not straddle z planes.
+static bool pipe_ok(const gpss_ctx *c, int axis)
+{
+    if (c->flags & GPSS_FLAG_NOPIPE) return false;
+    const int64_t n = c->n[axis];
+    if (n != 64 && n != 128 && n != 256) return false;
+    const int64_t W = 4096 / n;
+    const int64_t nlines = c->total / n;
+    if (nlines % W) return false;
+    if (axis == 1 && c->n[0] % W) return false;
+    return true;
+}
+
 template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const PassArgs<T> &a)
 {
+    if (mode == MODE_FUSED && pipe_ok(c, axis)) {
+        const int ntiles = (int)(c->total / c->n[axis] / (4096 / c->n[axis]));
+        cudaError_t e = PassLauncher<T>::pipe(axis == 0, (int)c->n[axis], a, ntiles, c->stream);
+        if (e != cudaSuccess)
+            return fail(c, GPSS_ECUDA, "pipelined pass launch (axis %d): %s", axis, cudaGetErrorString(e));
+        c->launches++;
+        return GPSS_OK;
+    }
     const int blocks = blocks_for<T>(c, axis);
     cudaError_t e = PassLauncher<T>::launch(mode, axis == 0, (int)c->n[axis], a, blocks, c->stream);
     if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "pass launch (axis %d, mode %d): %s", axis, mode,
@@ -248,24 +298,32 @@ template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const P
     return GPSS_OK;
 }
 
-static int finalize(gpss_ctx *c, int axis_blocks, int slot, int renorm)
+static const int kDiagSlot = 3;  // sums slot of read-only diagnostics (and the mass-lock target)
+
+// arm the in-kernel finish of a pass's reductions into sums slot `slot`
+template <typename T> static void set_finish(gpss_ctx *c, PassArgs<T> &a, int slot, int mode)
 {
     double dV = 1.0;
-    for (int a = 0; a < c->ndim; a++) dV *= c->d[a];
-    cudaError_t e = launch_finalize(c->partials, axis_blocks, RQ_COUNT, c->sums + slot * RQ_COUNT,
-                                    renorm, dV, c->scale, c->status, c->stream);
-    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "finalize launch: %s", cudaGetErrorString(e));
-    c->launches++;
-    return GPSS_OK;
+    for (int ax = 0; ax < c->ndim; ax++) dV *= c->d[ax];
+    a.partials = c->partials;
+    a.counter = c->counter;
+    a.fin_out = c->sums + slot * RQ_COUNT;
+    a.fin_mode = mode;
+    a.fin_target = c->sums + kDiagSlot * RQ_COUNT + RQ_MASS;
+    a.fin_scale = c->scale;
+    a.fin_status = c->status;
+    a.dV = dV;
 }
 
 // One kinetic flow L(dtl) as fused passes x, y[, z].  The last axis may carry
 // the nonlinear flow N(dtnl) as an epilogue and/or the pointwise reductions
-// (red_last); diag_kin adds the Parseval kinetic sums on every axis;
-// prescale multiplies the first pass's input by the device scalar c->scale.
+// (red_last, finished with fin_last: FIN_NONE, FIN_UNITMASS for the
+// imaginary-time renormalisation, FIN_MASSLOCK for restoring the mass of the
+// start of the call); diag_kin adds the Parseval kinetic sums on every axis;
+// prescale multiplies the first pass by the device scalar c->scale.
 template <typename T>
 static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl, int red_last,
-                         bool diag_kin, bool prescale)
+                         bool diag_kin, bool prescale, int fin_last = FIN_NONE)
 {
     for (int axis = 0; axis < c->ndim; axis++) {
         PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
@@ -286,9 +344,8 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
             a.red |= RED_KIN;
             a.coord = axis == 0 ? c->coord_dev[1] : (axis == 1 ? c->coord_dev[0] : nullptr);
         }
-        if (a.red) a.partials = c->partials;
+        if (a.red) set_finish<T>(c, a, axis, last ? fin_last : FIN_NONE);
         GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
-        if (a.red) GPSS_TRY(finalize(c, blocks_for<T>(c, axis), axis, imag && last && (red_last & RED_POINT)));
     }
     return GPSS_OK;
 }
@@ -323,8 +380,9 @@ template <typename T> static int nl_plain(gpss_ctx *c, double dt, int imag)
 }
 
 // sum |psi|^2 (and V|psi|^2, |psi|^4; with kin also the Parseval sums) of the
-// current field, read-only passes, into c->sums[slot axis]
-template <typename T> static int diag_passes(gpss_ctx *c, bool kin, int renorm)
+// current field by read-only passes, into c->sums slot `axis` (kin) or the
+// diagnostics slot (mass only)
+template <typename T> static int diag_passes(gpss_ctx *c, bool kin, int mode)
 {
     const int naxes = kin ? c->ndim : 1;
     for (int axis = 0; axis < naxes; axis++) {
@@ -332,9 +390,8 @@ template <typename T> static int diag_passes(gpss_ctx *c, bool kin, int renorm)
         a.red = (axis == 0 ? RED_POINT : 0) | (kin ? RED_KIN : 0);
         a.V = c->have_V ? (const T *)c->V : nullptr;
         a.coord = axis == 0 ? c->coord_dev[1] : (axis == 1 ? c->coord_dev[0] : nullptr);
-        a.partials = c->partials;
+        set_finish<T>(c, a, kin ? axis : kDiagSlot, axis == 0 ? mode : FIN_NONE);
         GPSS_TRY(launch<T>(c, axis, MODE_DIAG, a));
-        GPSS_TRY(finalize(c, blocks_for<T>(c, axis), axis, renorm && axis == 0));
     }
     return GPSS_OK;
 }
@@ -389,7 +446,7 @@ static int read_sums(gpss_ctx *c, double *h)
 
 template <typename T> static int energy_impl(gpss_ctx *c, double *out, double *mass)
 {
-    GPSS_TRY(diag_passes<T>(c, true, 0));
+    GPSS_TRY(diag_passes<T>(c, true, FIN_NONE));
     double h[4 * RQ_COUNT];
     GPSS_TRY(read_sums(c, h));
     if (!std::isfinite(h[RQ_MASS])) return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
@@ -404,6 +461,13 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
     const bool plain = (c->flags & GPSS_FLAG_PLAIN) != 0;
     const bool merge = !plain && !imag && scheme == GPSS_STRANG && c->omega == 0.0 &&
                        !(c->flags & GPSS_FLAG_NOMERGE);
+    // FP32 real time: restore the mass of the start of the call after every
+    // nonlinear stage (every stage is unitary, so in exact arithmetic the
+    // factor is 1; in FP32 it removes the drift that rounding feeds into the
+    // global phase through the nonlinear frequency beta |psi|^2)
+    const bool lock = !plain && !imag && c->precision == GPSS_FP32 && !(c->flags & GPSS_FLAG_NOMASSLOCK);
+    const int red_nl = lock ? RED_MASS : 0;
+    const int fin_nl = lock ? FIN_MASSLOCK : FIN_NONE;
     bool diag_done = false;
     if (nsteps == 0) {
         if (diag) {
@@ -412,10 +476,11 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         }
         return GPSS_OK;
     }
-    if (imag) {
+    if (imag || lock) {
         int zero = 0;
         CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     }
+    if (lock) GPSS_TRY(diag_passes<T>(c, false, FIN_NONE));  // target mass -> diagnostics slot
     if (plain) {
         for (int s = 0; s < nsteps; s++) {
             if (scheme == GPSS_STRANG) {
@@ -427,37 +492,48 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
                 GPSS_TRY(nl_plain<T>(c, dt, imag));
             }
             if (imag) {  // normalize! (Fields.jl:196-200)
-                GPSS_TRY(diag_passes<T>(c, false, 1));
+                GPSS_TRY(diag_passes<T>(c, false, FIN_UNITMASS));
                 GPSS_TRY(apply_scale<T>(c));
             }
         }
     } else if (merge) {
         // L(dt/2) N [L(dt) N]^(nsteps-1) L(dt/2): the kinetic flows of
         // consecutive steps commute (Omega = 0) and compose exactly.
-        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, 0, false, false));
-        for (int s = 1; s < nsteps; s++) GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, 0, false, false));
+        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, red_nl, false, false, fin_nl));
+        for (int s = 1; s < nsteps; s++)
+            GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, red_nl, false, lock, fin_nl));
         // final half step; with diag, the kinetic sums of each axis are exact
         // for the final field (real-time kinetic flows are unitary and commute
         // with the other axes' derivatives when Omega = 0)
-        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, diag ? RED_POINT : 0, diag != nullptr, false));
+        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, diag ? RED_POINT : 0, diag != nullptr, lock));
         diag_done = diag != nullptr;
-    } else {
+    } else if (imag) {
         for (int s = 0; s < nsteps; s++) {
-            const bool pre = imag && s > 0;
+            const bool pre = s > 0;
             if (scheme == GPSS_STRANG) {
-                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, imag, true, dt, 0, false, pre));
-                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, imag, false, 0.0, imag ? RED_POINT : 0, false, false));
+                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 1, true, dt, 0, false, pre));
+                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 1, false, 0.0, RED_MASS, false, false, FIN_UNITMASS));
             } else {
-                GPSS_TRY(kinetic_fused<T>(c, dt, imag, true, dt, imag ? RED_POINT : 0, false, pre));
+                GPSS_TRY(kinetic_fused<T>(c, dt, 1, true, dt, RED_MASS, false, pre, FIN_UNITMASS));
             }
         }
-        if (imag && nsteps > 0) GPSS_TRY(apply_scale<T>(c));
+        GPSS_TRY(apply_scale<T>(c));
+    } else {
+        for (int s = 0; s < nsteps; s++) {
+            if (scheme == GPSS_STRANG) {
+                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, red_nl, false, false, fin_nl));
+                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, 0, false, lock));
+            } else {
+                GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, red_nl, false, lock && s > 0, fin_nl));
+            }
+        }
     }
-    if (imag) {
+    if (imag || lock) {
         int st = 0;
         CUDA_TRY(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-        if (st) return fail(c, GPSS_ENONFINITE, "imaginary-time renormalisation saw a non-finite or zero mass");
+        if (st & 2) return fail(c, GPSS_ETIMEOUT, "a pipelined pass gave up waiting for a tile copy");
+        if (st) return fail(c, GPSS_ENONFINITE, "a renormalisation saw a non-finite or zero mass");
     }
     if (diag) {
         diag->steps = nsteps;
@@ -495,7 +571,8 @@ void gpss_destroy(gpss_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     clear_phases(c);
     void *ptrs[] = {c->psi, c->scratch, c->V, c->tw[0], c->tw[1], c->tw[2], c->coord_dev[0],
-                    c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status};
+                    c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status,
+                    c->counter};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : c->ev)
@@ -512,7 +589,7 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if (ndim != 2 && ndim != 3) return fail(nullptr, GPSS_EINVAL, "ndim must be 2 or 3 (got %d)", ndim);
     if (precision != GPSS_FP64 && precision != GPSS_FP32)
         return fail(nullptr, GPSS_EINVAL, "precision must be GPSS_FP64 or GPSS_FP32 (got %d)", precision);
-    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE))
+    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_NOPIPE))
         return fail(nullptr, GPSS_EINVAL, "unknown flags 0x%x", flags);
     for (int a = 0; a < ndim; a++) {
         if (!is_pow2(n[a]) || n[a] < 2 || n[a] > 256)
@@ -552,19 +629,22 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     int rc;
     if ((rc = dev_alloc(c, &c->psi, (size_t)c->total * cplx_bytes(c)))) return bail(rc);
     if ((rc = dev_alloc(c, &c->scratch, (size_t)c->total * 16))) return bail(rc);
-    // twiddles per axis, stage-A layout tw[k1*N2 + r] = exp(-2 pi i r k1 / n)
+    // twiddles per axis, stage-A layout m = k1*N2 + r: exp(-2 pi i r k1 / n) as hi + lo
     for (int a = 0; a < ndim; a++) {
         const int64_t na = c->n[a];
         const int64_t N1 = na <= 16 ? na : 16, N2 = na / N1;
-        std::vector<double> h((size_t)(2 * na));
+        // two rows: stage-A order (k1*N2 + r) and stage-B order (r*N1 + k1)
+        std::vector<ldouble> re((size_t)(2 * na)), im((size_t)(2 * na));
         for (int64_t k1 = 0; k1 < N1; k1++)
             for (int64_t r = 0; r < N2; r++) {
-                double cs, sn;
+                ldouble cs, sn;
                 unit_root(r * k1, na, &cs, &sn);
-                h[(size_t)(2 * (k1 * N2 + r))] = cs;
-                h[(size_t)(2 * (k1 * N2 + r) + 1)] = -sn;
+                re[(size_t)(k1 * N2 + r)] = cs;
+                im[(size_t)(k1 * N2 + r)] = -sn;
+                re[(size_t)(na + r * N1 + k1)] = cs;
+                im[(size_t)(na + r * N1 + k1)] = -sn;
             }
-        if ((rc = upload_table(c, &c->tw[a], h))) return bail(rc);
+        if ((rc = upload_dw(c, &c->tw[a], re, im, 2, na))) return bail(rc);
         if ((rc = dev_alloc(c, (void **)&c->coord_dev[a], sizeof(double) * (size_t)c->n[a]))) return bail(rc);
         e = cudaMemcpy(c->coord_dev[a], c->coord[a].data(), sizeof(double) * (size_t)c->n[a], cudaMemcpyHostToDevice);
         if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
@@ -579,6 +659,9 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if ((rc = dev_alloc(c, (void **)&c->sums, sizeof(double) * 4 * RQ_COUNT))) return bail(rc);
     if ((rc = dev_alloc(c, (void **)&c->scale, sizeof(double) * 2))) return bail(rc);
     if ((rc = dev_alloc(c, (void **)&c->status, sizeof(int) * 2))) return bail(rc);
+    if ((rc = dev_alloc(c, (void **)&c->counter, sizeof(unsigned int) * 2))) return bail(rc);
+    e = cudaMemset(c->counter, 0, sizeof(unsigned int) * 2);
+    if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemset: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
     double one = 1.0;
     e = cudaMemcpy(c->scale, &one, sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
@@ -679,12 +762,14 @@ static int raw_mass(gpss_ctx *c, double *out)
 {
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, 0) : diag_passes<double>(c, false, 0);
+    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, FIN_NONE)
+                                       : diag_passes<double>(c, false, FIN_NONE);
     if (rc) return rc;
     double h[4 * RQ_COUNT];
     GPSS_TRY(read_sums(c, h));
-    if (!std::isfinite(h[RQ_MASS])) return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
-    *out = h[RQ_MASS];
+    const double m = h[kDiagSlot * RQ_COUNT + RQ_MASS];
+    if (!std::isfinite(m)) return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
+    *out = m;
     return GPSS_OK;
 }
 
@@ -714,7 +799,8 @@ int gpss_normalize(gpss_ctx *c)
     CUDA_TRY(c, cudaSetDevice(c->device));
     int zero = 0;
     CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, 1) : diag_passes<double>(c, false, 1);
+    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, FIN_UNITMASS)
+                                       : diag_passes<double>(c, false, FIN_UNITMASS);
     if (rc) return rc;
     rc = c->precision == GPSS_FP32 ? apply_scale<float>(c) : apply_scale<double>(c);
     if (rc) return rc;

@@ -15,17 +15,28 @@ cudaError_t launch_pass_f64(int mode, bool xl, int n, const PassArgs<double> &a,
                             cudaStream_t s);
 int pass_lines_per_cta_f32(int n, bool xl);
 int pass_lines_per_cta_f64(int n, bool xl);
+// pipelined fused pass (n in {64, 128, 256}; tiles of 4096/n lines)
+cudaError_t launch_pipe_f32(bool xl, int n, const PassArgs<float> &a, int ntiles, cudaStream_t s);
+cudaError_t launch_pipe_f64(bool xl, int n, const PassArgs<double> &a, int ntiles, cudaStream_t s);
 
 template <typename T> struct PassLauncher;
 template <> struct PassLauncher<float> {
     static cudaError_t launch(int mode, bool xl, int n, const PassArgs<float> &a, int blocks,
                               cudaStream_t s) { return launch_pass_f32(mode, xl, n, a, blocks, s); }
     static int lines(int n, bool xl) { return pass_lines_per_cta_f32(n, xl); }
+    static cudaError_t pipe(bool xl, int n, const PassArgs<float> &a, int ntiles, cudaStream_t s)
+    {
+        return launch_pipe_f32(xl, n, a, ntiles, s);
+    }
 };
 template <> struct PassLauncher<double> {
     static cudaError_t launch(int mode, bool xl, int n, const PassArgs<double> &a, int blocks,
                               cudaStream_t s) { return launch_pass_f64(mode, xl, n, a, blocks, s); }
     static int lines(int n, bool xl) { return pass_lines_per_cta_f64(n, xl); }
+    static cudaError_t pipe(bool xl, int n, const PassArgs<double> &a, int ntiles, cudaStream_t s)
+    {
+        return launch_pipe_f64(xl, n, a, ntiles, s);
+    }
 };
 
 // pointwise kernels (pointwise.cu)
@@ -39,10 +50,4 @@ cudaError_t launch_nl(vec2<T> *psi, const T *V, double beta, double dt, int imag
                       cudaStream_t s);
 template <typename T>
 cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s);
-// sums partials[q * nblocks + b] over b for q < nq into out[q] (fixed order);
-// renorm != 0 also writes *scale_out = 1/sqrt(out[RQ_MASS] * dV) and sets
-// *status = 1 when the mass is not finite and positive.
-cudaError_t launch_finalize(const double *partials, int nblocks, int nq, double *out, int renorm,
-                            double dV, double *scale_out, int *status, cudaStream_t s);
-
 }  // namespace gpss

@@ -9,23 +9,42 @@
 // rate, so instead of FP64 the phase argument theta = (V + beta|psi|^2) dt is
 // formed in double-float arithmetic (an unevaluated sum of two floats,
 // ~48-bit significand; Dekker's two-product and Knuth's two-sum via FMA),
-// reduced modulo 2 pi with a three-term Cody-Waite split of 2 pi, and only
-// the reduced |r| <= pi is rounded to one float for sincosf.  The error of the
-// reduced argument is therefore about one float ulp of r, independent of how
-// large theta is.
+// reduced modulo pi/2 with a three-term Cody-Waite split of pi/2, and only
+// the reduced |f| <= pi/4 is rounded to one float.  sin f and cos f then come
+// from their Taylor series (degree 9 and 10: truncation below 3e-9 relative
+// on |f| <= pi/4, under half an FP32 ulp) and the quadrant.  The error of the
+// reduced argument is about one float ulp of f, whatever the size of theta.
 #pragma once
 #include <cuda_runtime.h>
 #include "fft_core.cuh"
 
 namespace gpss {
 
-// 2 pi = PI2_A + PI2_B + PI2_C (floats; residual ~4e-23)
-#define GPSS_PI2_A 6.2831854820251465f
-#define GPSS_PI2_B (-1.7484555314695172e-07f)
-#define GPSS_PI2_C (-6.8604980400235275e-15f)
-#define GPSS_INV_PI2 0.15915493667125702f
+// pi/2 = PIO2_A + PIO2_B + PIO2_C (floats; residual ~1e-23)
+#define GPSS_PIO2_A 1.5707963705062866f
+#define GPSS_PIO2_B (-4.371138828673793e-08f)
+#define GPSS_PIO2_C (-1.7151245100058819e-15f)
+#define GPSS_TWO_OVER_PI 0.6366197466850281f
 
 struct DF { float hi, lo; };
+
+// sin f and cos f for |f| <= pi/4 from the Taylor series
+//   sin f = f - f^3/3! + f^5/5! - f^7/7! + f^9/9!
+//   cos f = 1 - f^2/2! + f^4/4! - f^6/6! + f^8/8! - f^10/10!
+// evaluated by Horner's rule in f^2.
+__device__ __forceinline__ void sincos_reduced(float f, float *s, float *c)
+{
+    const float z = f * f;
+    float ps = fmaf(z, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps = fmaf(z, ps, 1.0f / 120.0f);
+    ps = fmaf(z, ps, -1.0f / 6.0f);
+    *s = fmaf(f * z, ps, f);
+    float pc = fmaf(z, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = fmaf(z, pc, -1.0f / 720.0f);
+    pc = fmaf(z, pc, 1.0f / 24.0f);
+    pc = fmaf(z, pc, -0.5f);
+    *c = fmaf(z, pc, 1.0f);
+}
 
 __device__ __forceinline__ DF two_prod(float a, float b)
 {
@@ -90,15 +109,23 @@ __device__ __forceinline__ float2 nl_apply(float2 v, float Vv, const NLConst<flo
     // theta = s * dt
     DF th = two_prod(s.hi, c.dh);
     th.lo += s.hi * c.dl + s.lo * c.dh;
-    // reduce theta modulo 2 pi (the first FMA is exact)
-    const float k = rintf(th.hi * GPSS_INV_PI2);
-    const float r1 = fmaf(-k, GPSS_PI2_A, th.hi);
-    float corr = fmaf(-k, GPSS_PI2_B, th.lo);
-    corr = fmaf(-k, GPSS_PI2_C, corr);
-    const float red = r1 + corr;
-    float sn, cs;
-    sincosf(-red, &sn, &cs);
-    return make_float2(cs * v.x - sn * v.y, cs * v.y + sn * v.x);
+    // reduce theta modulo pi/2 (the first FMA is exact: both terms are
+    // multiples of the ulp of PIO2_A and the result is below 1 in magnitude)
+    const float k = rintf(th.hi * GPSS_TWO_OVER_PI);
+    const float r1 = fmaf(-k, GPSS_PIO2_A, th.hi);
+    float corr = fmaf(-k, GPSS_PIO2_B, th.lo);
+    corr = fmaf(-k, GPSS_PIO2_C, corr);
+    const float f = r1 + corr;
+    float sf, cf;
+    sincos_reduced(f, &sf, &cf);
+    // sin/cos of theta from the quadrant q = k mod 4
+    const int quad = ((int)k) & 3;
+    float st = (quad & 1) ? cf : sf;
+    float ct = (quad & 1) ? sf : cf;
+    if (quad == 1 || quad == 2) ct = -ct;
+    if (quad >= 2) st = -st;
+    // psi * exp(-i theta)
+    return make_float2(ct * v.x + st * v.y, ct * v.y - st * v.x);
 }
 
 }  // namespace gpss

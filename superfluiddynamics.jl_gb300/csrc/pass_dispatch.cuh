@@ -2,6 +2,7 @@
 // the pass_kernel instantiation.  Included once per precision.
 #pragma once
 #include "pass_kernel.cuh"
+#include "pass_pipe.cuh"
 
 namespace gpss {
 
@@ -10,8 +11,9 @@ static cudaError_t launch_pass_inst(const PassArgs<T> &a, int blocks, cudaStream
 {
     using S = PassShape<T, N, XL>;
     auto k = pass_kernel<T, N, XL, MODE>;
-    if (S::SMEM_BYTES > 48 * 1024) {
-        // opt-in for more than 48 KB of dynamic shared memory (per device)
+    {
+        // opt in to the dynamic shared memory this instantiation needs (the
+        // default limit counts dynamic + static bytes against 48 KB), once per device
         static bool done[64] = {false};
         int dev = 0;
         cudaGetDevice(&dev);
@@ -45,12 +47,53 @@ static cudaError_t launch_pass_n(int mode, bool xl, const PassArgs<T> &a, int bl
               : launch_pass_mode<T, N, false>(mode, a, blocks, s);
 }
 
+template <typename T, int N, bool XL>
+static cudaError_t launch_pipe_inst(const PassArgs<T> &a, int ntiles, cudaStream_t s)
+{
+    using S = PipeShape<T, N, XL>;
+    auto k = pass_pipe_kernel<T, N, XL>;
+    static int blocks_per_sm[64] = {0};
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int d = (dev >= 0 && dev < 64) ? dev : 0;
+    if (!blocks_per_sm[d] || dev != d) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        int nb = 0, nsm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, S::THREADS, S::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        if (nb < 1) return cudaErrorInvalidConfiguration;
+        blocks_per_sm[d] = nb;
+        sms[d] = nsm;
+    }
+    int grid = blocks_per_sm[d] * sms[d];
+    if (grid > ntiles) grid = ntiles;
+    k<<<grid, S::THREADS, S::SMEM_BYTES, s>>>(a, ntiles);
+    return cudaGetLastError();
+}
+
 template <typename T, int N> static int lines_per_cta_n(bool xl)
 {
     return xl ? PassShape<T, N, true>::W : PassShape<T, N, false>::W;
 }
 
 #define GPSS_DEFINE_PASS_DISPATCH(T, SUFFIX)                                                   \
+    cudaError_t launch_pipe_##SUFFIX(bool xl, int n, const PassArgs<T> &a, int ntiles,         \
+                                     cudaStream_t s)                                           \
+    {                                                                                          \
+        switch (n) {                                                                           \
+        case 64: return xl ? launch_pipe_inst<T, 64, true>(a, ntiles, s)                       \
+                           : launch_pipe_inst<T, 64, false>(a, ntiles, s);                     \
+        case 128: return xl ? launch_pipe_inst<T, 128, true>(a, ntiles, s)                     \
+                            : launch_pipe_inst<T, 128, false>(a, ntiles, s);                   \
+        case 256: return xl ? launch_pipe_inst<T, 256, true>(a, ntiles, s)                     \
+                            : launch_pipe_inst<T, 256, false>(a, ntiles, s);                   \
+        default: return cudaErrorInvalidValue;                                                 \
+        }                                                                                      \
+    }                                                                                          \
     cudaError_t launch_pass_##SUFFIX(int mode, bool xl, int n, const PassArgs<T> &a,           \
                                      int blocks, cudaStream_t s)                               \
     {                                                                                          \

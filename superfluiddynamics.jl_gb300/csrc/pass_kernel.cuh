@@ -32,6 +32,10 @@
 // Shared-memory layouts are chosen so every stage is bank-conflict free
 // (XL: one pad slot per N2-row plus N2 per line; COL: position-major).
 //
+// Constants (twiddles w_n^{r k1} and the kinetic phase factors) are held as
+// double-word pairs hi + lo and applied with cmul2: a rounded constant alone
+// would repeat the same relative error on the same mode at every pass.
+//
 // Modes:
 //   MODE_FUSED  FFT -> phase -> iFFT (+ optional NL epilogue, reductions)
 //   MODE_FWD    FFT only, writes the natural-order spectrum (plain form)
@@ -55,14 +59,22 @@ enum {
     RQ_ROT = 4,    // sum over lines of c_line (1/n) sum_k xi_k |X_k|^2
     RQ_COUNT = 5
 };
-enum { RED_POINT = 1, RED_KIN = 2 };
+enum { RED_POINT = 1, RED_KIN = 2, RED_MASS = 4 };
+// how the last CTA finishes a reduction: plain sums, plus the factor of the
+// imaginary-time renormalisation (1/sqrt(M dV), normalize!) or of the mass
+// lock (sqrt(M0/M)) written to *fin_scale for the next pass
+enum { FIN_NONE = 0, FIN_UNITMASS = 1, FIN_MASSLOCK = 2 };
 enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 
 template <typename T> struct PassArgs {
     const vec2<T> *in;
     vec2<T> *out;
-    const vec2<T> *tw;       // n entries, stage-A layout: tw[k1*N2 + r] = w_n^{r k1}
-    const vec2<T> *phase;    // phase[k + row*prow] (already includes 1/n in fused mode)
+    const vec2<T> *tw;       // 4n entries: stage-A table hi[n], lo[n] at m = k1*N2 + r, then
+                             // the stage-B table hi[n], lo[n] at m = r*N1 + k1; both hold
+                             // hi[m] + lo[m] = w_n^{r k1} (two index orders so that adjacent
+                             // lanes read adjacent entries in either stage)
+    const vec2<T> *phase;    // per row: hi[n] then lo[n]; row `row` starts at row*prow
+                             // (fused tables already include the 1/n of the inverse)
     int64_t prow;            // 0: one table row for every line (held in shared memory)
     int rowmod;              // row of line g is g % rowmod
     int nlines;
@@ -75,9 +87,16 @@ template <typename T> struct PassArgs {
     double nl_beta, nl_dt;
     // deferred renormalisation: multiply the input by *scale (nullable)
     const double *scale;
-    // reductions
-    int red;                 // RED_POINT | RED_KIN
+    // reductions: per-CTA FP64 partials, finished by the last CTA to arrive
+    int red;                 // RED_POINT | RED_KIN | RED_MASS
     double *partials;        // [RQ_COUNT][gridDim.x]
+    unsigned int *counter;   // arrival counter (0 between launches)
+    double *fin_out;         // RQ_COUNT sums of this pass
+    int fin_mode;            // FIN_*
+    const double *fin_target;  // M0 of the mass lock
+    double *fin_scale;       // factor for the next pass
+    int *fin_status;         // set to 1 on a non-finite or non-positive mass
+    double dV;
     double kmult;            // xi_k = kk * kmult, kk the signed wavenumber index
     const double *coord;     // coordinate of each row (rotation energy), nullable
 };
@@ -99,7 +118,7 @@ template <typename T, int N, bool XL> struct PassShape {
     static constexpr int W = THREADS / P;              // lines per CTA
     static constexpr int LS = N + N1 + N2;             // XL padded line stride (slots)
     static constexpr int DATA = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
-    static constexpr int SMEM_SLOTS = DATA + 2 * N;    // + twiddle + phase tables
+    static constexpr int SMEM_SLOTS = DATA + 6 * N;    // + twiddles (A, B) + phase, hi and lo
     static constexpr size_t SMEM_BYTES = sizeof(vec2<T>) * SMEM_SLOTS;
 };
 
@@ -121,6 +140,53 @@ __device__ __forceinline__ void block_sum_store(T v, double *partials, int q, T 
     }
 }
 
+// The last CTA of the grid to finish sums every CTA's partials (same fixed
+// order whichever CTA is last, so results are deterministic), writes the
+// sums and the next-pass factor, and re-arms the counter for the next launch.
+template <typename T, int THREADS>
+__device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned qmask)
+{
+    __shared__ bool last;
+    __shared__ double red[THREADS];
+    if (threadIdx.x == 0) {
+        __threadfence();  // this CTA's partials before its arrival
+        const unsigned ticket = atomicAdd(a.counter, 1u);
+        last = ticket == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int G = gridDim.x;
+    for (int q = 0; q < RQ_COUNT; q++) {
+        if (!(qmask & (1u << q))) continue;
+        double s = 0.0;
+        for (int b = threadIdx.x; b < G; b += THREADS) s += __ldcg(a.partials + (size_t)q * G + b);
+        red[threadIdx.x] = s;
+        __syncthreads();
+#pragma unroll
+        for (int o = THREADS / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) a.fin_out[q] = red[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (a.fin_mode != FIN_NONE) {
+            const double m = a.fin_out[RQ_MASS];
+            if (!(m > 0.0) || !isfinite(m)) {
+                *a.fin_status = 1;
+                *a.fin_scale = 1.0;
+            } else if (a.fin_mode == FIN_MASSLOCK) {
+                *a.fin_scale = sqrt(*a.fin_target / m);
+            } else {
+                *a.fin_scale = 1.0 / (sqrt(m) * sqrt(a.dV));
+            }
+        }
+        *a.counter = 0u;
+    }
+}
+
 template <typename T, int N, bool XL, int MODE>
 __global__ void __launch_bounds__(PassGeom<T>::THREADS)
 pass_kernel(const PassArgs<T> a)
@@ -132,15 +198,15 @@ pass_kernel(const PassArgs<T> a)
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *sdata = reinterpret_cast<V *>(smem_raw);
-    V *stw = sdata + S::DATA;
-    V *sph = stw + N;
+    V *stw = sdata + S::DATA;  // stage A: hi[N], lo[N]; stage B: hi[N], lo[N]
+    V *stwB = stw + 2 * N;
+    V *sph = stw + 4 * N;      // hi[N], lo[N]
 
     const int tid = threadIdx.x;
     // tables into shared memory
-    for (int i = tid; i < N; i += THREADS) {
-        stw[i] = a.tw[i];
-        if (MODE == MODE_FUSED && a.prow == 0) sph[i] = a.phase[i];
-    }
+    for (int i = tid; i < 4 * N; i += THREADS) stw[i] = a.tw[i];
+    if (MODE == MODE_FUSED && a.prow == 0)
+        for (int i = tid; i < 2 * N; i += THREADS) sph[i] = a.phase[i];
 
     const int w = XL ? tid / P : tid % W;
     const int r = XL ? tid % P : tid / W;
@@ -156,8 +222,8 @@ pass_kernel(const PassArgs<T> a)
         else return q * W + w;
     };
 
-    T scale = (T)1;
-    if (a.scale) scale = (T)(*a.scale);
+    const bool scaled = a.scale != nullptr;
+    const T scale = scaled ? (T)(*a.scale) : (T)1;
     const T kmult = (T)a.kmult;
 
     // accumulators (precision of the field; the CTA totals are kept in FP64)
@@ -202,8 +268,10 @@ pass_kernel(const PassArgs<T> a)
             }
 #pragma unroll
             for (int k = 0; k < N1; k++) {
-                V ph = a.prow ? a.phase[k + row * a.prow] : sph[k];
-                v[k] = cmul(v[k], cscale(ph, scale));
+                const V ph = a.prow ? a.phase[row * a.prow + k] : sph[k];
+                const V pl = a.prow ? a.phase[row * a.prow + N + k] : sph[N + k];
+                v[k] = cmul2(v[k], ph, pl);
+                if (scaled) v[k] = cscale(v[k], scale);
             }
             dft<N1, +1>(v);
         } else if constexpr (MODE == MODE_DIAG) {
@@ -235,8 +303,9 @@ pass_kernel(const PassArgs<T> a)
         if constexpr (MODE != MODE_INV) {
 #pragma unroll
             for (int k1 = 0; k1 < N1; k1++) {
-                V t = k1 == 0 ? v[k1] : cmul(v[k1], stw[k1 * N2 + r]);
-                sdata[sidx(k1 * N2 + r)] = t;
+                const int m = k1 * N2 + r;
+                V t = (k1 == 0 || r == 0) ? v[k1] : cmul2(v[k1], stw[m], stw[N + m]);
+                sdata[sidx(m)] = t;
             }
             __syncthreads();
         }
@@ -283,14 +352,17 @@ pass_kernel(const PassArgs<T> a)
 #pragma unroll
                 for (int k2 = 0; k2 < N2; k2++) {
                     const int k = k1 + N1 * k2;
-                    V ph = a.prow ? a.phase[k + row * a.prow] : sph[k];
-                    u[k2] = cmul(u[k2], cscale(ph, scale));
+                    const V ph = a.prow ? a.phase[row * a.prow + k] : sph[k];
+                    const V pl = a.prow ? a.phase[row * a.prow + N + k] : sph[N + k];
+                    u[k2] = cmul2(u[k2], ph, pl);
+                    if (scaled) u[k2] = cscale(u[k2], scale);
                 }
             }
             dft<N2, +1>(u);  // u[rr] = Z[k1][rr]
 #pragma unroll
             for (int rr = 0; rr < N2; rr++) {
-                V t = (k1 == 0 || rr == 0) ? u[rr] : cmulc(u[rr], stw[k1 * N2 + rr]);
+                const int mb = rr * N1 + k1;
+                V t = (k1 == 0 || rr == 0) ? u[rr] : cmulc2(u[rr], stwB[mb], stwB[N + mb]);
                 sdata[sidx(k1 * N2 + rr)] = t;
             }
         }
@@ -327,6 +399,9 @@ pass_kernel(const PassArgs<T> a)
                     acc_int += rho * rho;
                     if (a.V && valid) acc_pot += a.V[base + (int64_t)(r + N2 * j) * st] * rho;
                 }
+            } else if (a.red & RED_MASS) {
+#pragma unroll
+                for (int j = 0; j < N1; j++) acc_mass += v[j].x * v[j].x + v[j].y * v[j].y;
             }
         }
         if (valid) {
@@ -344,8 +419,9 @@ pass_kernel(const PassArgs<T> a)
         if (a.red) {
             __shared__ T red_smem[THREADS / 32];
             if (!valid) { acc_mass = acc_pot = acc_int = acc_kin = acc_rot = 0; }
-            if (a.red & RED_POINT) {
+            if (a.red & (RED_POINT | RED_MASS))
                 block_sum_store<T, THREADS>(acc_mass, a.partials, RQ_MASS, red_smem);
+            if (a.red & RED_POINT) {
                 block_sum_store<T, THREADS>(acc_pot, a.partials, RQ_POT, red_smem);
                 block_sum_store<T, THREADS>(acc_int, a.partials, RQ_INT, red_smem);
             }
@@ -353,6 +429,11 @@ pass_kernel(const PassArgs<T> a)
                 block_sum_store<T, THREADS>(acc_kin, a.partials, RQ_KIN, red_smem);
                 block_sum_store<T, THREADS>(acc_rot, a.partials, RQ_ROT, red_smem);
             }
+            unsigned qmask = 0;
+            if (a.red & (RED_POINT | RED_MASS)) qmask |= 1u << RQ_MASS;
+            if (a.red & RED_POINT) qmask |= (1u << RQ_POT) | (1u << RQ_INT);
+            if (a.red & RED_KIN) qmask |= (1u << RQ_KIN) | (1u << RQ_ROT);
+            finish_reduction<T, THREADS>(a, qmask);
         }
     }
 }

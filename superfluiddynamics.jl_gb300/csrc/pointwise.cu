@@ -1,6 +1,6 @@
 // pointwise.cu -- element-wise kernels: precision conversion at the host
-// boundary, the plain-form phase multiply and nonlinear step, deferred
-// renormalisation, and the fixed-order finish of the CTA-partial reductions.
+// boundary, the plain-form phase multiply and nonlinear step, and the
+// scaling that applies a renormalisation factor left on the device.
 #include "gpss_internal.h"
 
 namespace gpss {
@@ -40,11 +40,12 @@ cudaError_t launch_f32_to_f64(const float *in, double *out, int64_t count, cudaS
     return cudaGetLastError();
 }
 
-// Plain form: psi_hat(k, row) *= phase[k + row * prow] on a natural-order
-// spectrum along `axis` (the broadcasts of splitting.jl:167/172/190/195/200).
+// Plain form: psi_hat(k, row) *= phase(k, row) on a natural-order spectrum
+// along `axis` (the broadcasts of splitting.jl:167/172/190/195/200).  Table
+// rows are hi[n] then lo[n] (double-word factors); row `row` starts at row*prow.
 template <typename T>
 __global__ void k_mul_phase(vec2<T> *__restrict__ data, const vec2<T> *__restrict__ phase,
-                            int64_t prow, int axis, int64_t nx, int64_t ny, int64_t total)
+                            int64_t prow, int axis, int64_t nx, int64_t ny, int64_t nk, int64_t total)
 {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -52,7 +53,8 @@ __global__ void k_mul_phase(vec2<T> *__restrict__ data, const vec2<T> *__restric
         if (axis == 0) { k = e % nx; row = (e / nx) % ny; }
         else if (axis == 1) { k = (e / nx) % ny; row = e % nx; }
         else { k = e / (nx * ny); row = 0; }
-        data[e] = cmul(phase[k + row * prow], data[e]);
+        const vec2<T> *p = phase + row * prow;
+        data[e] = cmul2(data[e], p[k], p[nk + k]);
     }
 }
 
@@ -60,7 +62,8 @@ template <typename T>
 cudaError_t launch_mul_phase(vec2<T> *data, const vec2<T> *phase, int64_t prow, int axis,
                              const int64_t *n, int64_t total, cudaStream_t s)
 {
-    k_mul_phase<T><<<grid_for(total, 256), 256, 0, s>>>(data, phase, prow, axis, n[0], n[1], total);
+    k_mul_phase<T><<<grid_for(total, 256), 256, 0, s>>>(data, phase, prow, axis, n[0], n[1], n[axis],
+                                                        total);
     return cudaGetLastError();
 }
 
@@ -98,41 +101,6 @@ template <typename T>
 cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s)
 {
     k_scale<T><<<grid_for(total, 256), 256, 0, s>>>(psi, scale, total);
-    return cudaGetLastError();
-}
-
-__global__ void k_finalize(const double *__restrict__ partials, int nblocks, int nq,
-                           double *__restrict__ out, int renorm, double dV,
-                           double *__restrict__ scale_out, int *__restrict__ status)
-{
-    __shared__ double sh[256];
-    for (int q = 0; q < nq; q++) {
-        double s = 0.0;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(size_t)q * nblocks + b];
-        sh[threadIdx.x] = s;
-        __syncthreads();
-        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-            if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) out[q] = sh[0];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0 && renorm) {
-        const double m = out[RQ_MASS];
-        if (!(m > 0.0) || !isfinite(m)) {
-            if (status) *status = 1;
-            *scale_out = 1.0;
-        } else {
-            *scale_out = 1.0 / (sqrt(m) * sqrt(dV));
-        }
-    }
-}
-
-cudaError_t launch_finalize(const double *partials, int nblocks, int nq, double *out, int renorm,
-                            double dV, double *scale_out, int *status, cudaStream_t s)
-{
-    k_finalize<<<1, 256, 0, s>>>(partials, nblocks, nq, out, renorm, dV, scale_out, status);
     return cudaGetLastError();
 }
 

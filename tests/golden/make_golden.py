@@ -1,6 +1,11 @@
 """Generates the golden vectors of tests/golden/*.npz with the CPU oracle
 (oracle/gp_oracle.c), cross-checked against the independent numpy restatement
-before writing.  Run from the repository root:  python tests/golden/make_golden.py
+before writing.  Each file holds the input, the FP64 oracle's output `psi`
+and the long-double oracle's output `psi_ext` (a near-exact reference: FP64
+implementations differ from it only by their own round-off).
+
+Run from the repository root on an x86 host (80-bit long double):
+    python tests/golden/make_golden.py
 """
 import math
 import os
@@ -48,6 +53,15 @@ def cases():
     yield "split2_3d_imag_rot", dict(psi0=field((16, 16, 8), 3), bounds=b, V=O.quadratic_potential((16, 16, 8), b),
                                      coeffD=-0.5, beta=50.0, omega=0.3, nsteps=20, scheme=2, imag=True, dt=1e-2)
     b = ((0.0, 2 * math.pi),) * 3
+    # cfg0 at full size: 2D 128^2 trap, g = 500, 1000 steps (the FP64 parity run)
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as g
+    g.load_package()
+    import importlib
+    c0 = importlib.import_module("sfd_gb300.workloads").cfg0()
+    yield "cfg0_2d_128_1000", dict(psi0=c0["psi"], bounds=c0["bounds"], V=c0["V"], coeffD=c0["coeffD"],
+                                   beta=c0["beta"], omega=0.0, nsteps=c0["nsteps"], scheme=2, imag=False,
+                                   dt=c0["dt"])
     yield "split2_3d_periodic_box", dict(psi0=np.asfortranarray(np.exp(1j * field((16, 16, 16), 4).real)),
                                          bounds=b, V=None, coeffD=-0.05 / math.sqrt(2),
                                          beta=1 / (math.sqrt(2) * 0.05), omega=0.0, nsteps=20, scheme=2,
@@ -59,15 +73,17 @@ def main():
         kw = dict(coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"], nsteps=c["nsteps"],
                   scheme=c["scheme"], imag=c["imag"], dt=c["dt"])
         out = O.c_step(c["psi0"], c["bounds"], **kw)
+        ext = O.c_step(c["psi0"], c["bounds"], extended=True, **kw)
         chk = O.np_step(c["psi0"], c["bounds"], **kw)
-        assert O.rel_l2(out, chk) < 1e-13, name
+        assert O.rel_l2(out, chk) < 4e-12, name
         e = O.c_energy(out, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"])
         V = c["V"] if c["V"] is not None else np.zeros(c["psi0"].shape)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), psi0=c["psi0"], psi=out, V=V,
                             has_V=c["V"] is not None, bounds=np.array(c["bounds"]), coeffD=c["coeffD"],
                             beta=c["beta"], omega=c["omega"], nsteps=c["nsteps"], scheme=c["scheme"],
-                            imag=c["imag"], dt=c["dt"], energy=np.array(e))
-        print(name, out.shape, "numpy cross-check", O.rel_l2(out, chk))
+                            imag=c["imag"], dt=c["dt"], energy=np.array(e), psi_ext=ext)
+        print(name, out.shape, "numpy vs FP64 oracle", O.rel_l2(out, chk), "FP64 oracle vs extended",
+              O.rel_l2(out, ext))
 
 
 if __name__ == "__main__":

@@ -47,7 +47,7 @@ def _create(L, ndim, n, lo, hi, prec=64, flags=0):
     (2, (1, 32), (0, 0), (1, 1), 64, 0),        # below 2
     (2, (32, 32), (1, 0), (1, 1), 64, 0),       # lo == hi
     (2, (32, 32), (0, 0), (1, 1), 16, 0),       # unknown precision
-    (3, (8, 8, 8), (0, 0, 0), (1, 1, 1), 32, 8),  # unknown flag
+    (3, (8, 8, 8), (0, 0, 0), (1, 1, 1), 32, 64),  # unknown flag
 ])
 def test_create_rejects_bad_arguments(L, ndim, n, lo, hi, prec, flags):
     rc, h = _create(L, ndim, n, lo, hi, prec, flags)

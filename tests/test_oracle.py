@@ -173,6 +173,8 @@ def test_golden_fixtures_reproduce(O):
                        omega=float(z["omega"]), V=V, nsteps=int(z["nsteps"]), scheme=int(z["scheme"]),
                        imag=bool(z["imag"]), dt=float(z["dt"]))
         assert O.rel_l2(out, z["psi"]) < 1e-13, nm
+        # the FP64 oracle's own distance to the long-double reference
+        assert O.rel_l2(z["psi"], z["psi_ext"]) < 1e-12, nm
         e = O.c_energy(z["psi"], b, coeffD=float(z["coeffD"]), beta=float(z["beta"]),
                        omega=float(z["omega"]), V=V)
         assert np.allclose(e, z["energy"], rtol=1e-12, atol=1e-14), nm
