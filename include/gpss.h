@@ -166,6 +166,29 @@ int gpss_host_free(void *ptr);
 /* Device memory held by the context, in bytes. */
 int64_t gpss_device_bytes(const gpss_ctx *ctx);
 
+/*
+ * Energies of a field that already lives in the caller's device memory,
+ * computed without any allocation by the library.  No counterpart in the
+ * reference: it exists for callers that cannot let the library cudaMalloc --
+ * for example a Julia session whose CuArrays come from CUDA.jl's memory pool,
+ * or a program held to a fixed device-memory budget.
+ *   psi_dev  device pointer, n[0]*n[1][*n[2]] complex values, x fastest
+ *            (double2 for GPSS_FP64, float2 for GPSS_FP32)
+ *   V_dev    device pointer to the real potential in the same precision, or NULL
+ *   stream   cudaStream_t to run on (NULL: the default stream); the call
+ *            returns after the stream has finished its work
+ *   out      host array of 5 doubles: E_Omega, E_Delta, E_beta, E, mu (as gpss_energy)
+ * Scratch lives in a 1 MiB device array inside the library, held by every GPU
+ * that loads it until the process exits.  Fields whose largest reduction
+ * needs more partial sums than fit are rejected with GPSS_EINVAL (256^3 fits).
+ * The first call on a device looks that array up; make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race, so
+ * serialise them.  Returns 0 or a negative GPSS_E* code (no message).
+ */
+int gpss_energy_noalloc(int ndim, const int64_t *n, const double *lo, const double *hi, int precision,
+                        double coeffD, double beta, double omega, const void *psi_dev, const void *V_dev,
+                        void *stream, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,6 +81,8 @@ SIGNATURES = {
     "gpss_host_alloc": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int64]),
     "gpss_host_free": (ctypes.c_int, [_vp]),
     "gpss_device_bytes": (ctypes.c_int64, [_vp]),
+    "gpss_energy_noalloc": (ctypes.c_int, [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _f64p]),
 }
 
 _lib = None
