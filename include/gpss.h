@@ -128,6 +128,20 @@ int gpss_normalize(gpss_ctx *ctx);
 int gpss_ground_state(gpss_ctx *ctx, double dt, double tol, int64_t max_steps, int check_every,
                       double *mu_out, int64_t *steps_out);
 
+/*
+ * Discrete adjoint of nsteps real-time Strang steps from the current field
+ * (an extension: the reference has no gradient path).  Loss
+ *     L = 1 - |<psi_target, psi(T)>|^2,   <a, b> = sum conj(a) b dV.
+ * Returns L, dLdV[cell] = dL/dV(cell) (FP64, field shape, nullable) and
+ * dLdpsi0 = 2 dL/d conj(psi0) (interleaved complex doubles, nullable; so that
+ * dL = Re sum conj(dLdpsi0) dpsi0).  The forward states are checkpointed every
+ * K steps and recomputed segment by segment.  FP32 contexts run the forward and
+ * the adjoint field in FP32 and accumulate dL/dV in FP64.  The context's
+ * field is left at psi0.
+ */
+int gpss_adjoint(gpss_ctx *ctx, const double *psi_target, int nsteps, int K, double dt, double *loss,
+                 double *dLdV, double *dLdpsi0);
+
 /* ---- timing and integration helpers (no reference counterpart) ---- */
 
 /* Make `device` the CUDA device that later gpss_create calls on this host

@@ -256,3 +256,47 @@ def relerr_max(a, b) -> float:
     """Max-norm relative error, test/runtests.jl:5."""
     a = np.asarray(a); b = np.asarray(b)
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+# ------------------------------------------------- forward-mode (dual numbers) --
+def np_tangent_loss(psi0, dpsi0, V, dV, psi_target, bounds, *, coeffD=-0.5, beta=1.0, nsteps=1, dt=1e-3):
+    """Loss L = 1 - |<psi_target, psi(T)>|^2 of nsteps real-time Strang steps
+    (splitting.jl:149-209, Omega = 0) and its directional derivative along
+    (dpsi0, dV), by dual numbers: every value carries a tangent, the FFT stages
+    are linear (the tangent goes through the same transform), the nonlinear
+    stage psi_out = exp(-i theta) psi with theta = (V + beta|psi|^2) dt gives
+    dpsi_out = exp(-i theta) (dpsi - i dtheta psi),
+    dtheta = (dV + 2 beta Re(conj(psi) dpsi)) dt.  Returns (L, dL)."""
+    p = np.array(psi0, dtype=np.complex128, order="F", copy=True)
+    t = np.array(dpsi0, dtype=np.complex128, order="F", copy=True)
+    nd = p.ndim
+    shape = p.shape
+    d = spacing(shape, bounds)
+    xis = [fftfreq(n, dd) for n, dd in zip(shape, d)]
+    Vv = np.zeros(shape) if V is None else np.asarray(V, dtype=np.float64)
+    dVv = np.zeros(shape) if dV is None else np.asarray(dV, dtype=np.float64)
+
+    def lap(dtl):
+        for a in range(nd):
+            s = [1] * nd
+            s[a] = shape[a]
+            xi = xis[a].reshape(s)
+            fac = np.exp(1j * ((coeffD * (xi * xi)) * dtl))
+            p[...] = np.fft.ifft(fac * np.fft.fft(p, axis=a), axis=a)
+            t[...] = np.fft.ifft(fac * np.fft.fft(t, axis=a), axis=a)
+
+    for _ in range(nsteps):
+        lap(dt * 0.5)
+        rho = p.real ** 2 + p.imag ** 2
+        theta = (Vv + beta * rho) * dt
+        dtheta = (dVv + 2.0 * beta * (p.real * t.real + p.imag * t.imag)) * dt
+        f = np.exp(-1j * theta)
+        t[...] = f * (t - 1j * dtheta * p)
+        p[...] = f * p
+        lap(dt * 0.5)
+    cell = float(np.prod(d))
+    z = np.sum(np.conj(psi_target) * p) * cell
+    dz = np.sum(np.conj(psi_target) * t) * cell
+    L = 1.0 - abs(z) ** 2
+    dL = -2.0 * float(np.real(np.conj(z) * dz))
+    return float(L), dL

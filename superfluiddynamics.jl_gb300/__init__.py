@@ -322,6 +322,20 @@ class _SplitModel:
         self._device_newer = True
         return mu.value, steps.value
 
+    def adjoint(self, psi_target, nsteps, K=50):
+        """Loss L = 1 - |<psi_target, psi(T)>|^2 after nsteps Strang steps from
+        the current field, with dL/dV (real, field shape) and the Wirtinger
+        gradient 2 dL/d conj(psi0).  The field is left unchanged."""
+        tgt = np.asfortranarray(np.asarray(psi_target, dtype=np.complex128))
+        if tgt.shape != self.f.g.n:
+            raise ValueError("psi_target must have the field's shape")
+        loss = ctypes.c_double()
+        dv = np.zeros(self.f.g.n, dtype=np.float64, order="F")
+        gp = np.zeros(self.f.g.n, dtype=np.complex128, order="F")
+        self._ck(_lib.lib().gpss_adjoint(self._h, tgt.ctypes.data_as(_f64p), int(nsteps), int(K), self.dt,
+                                         ctypes.byref(loss), dv.ctypes.data_as(_f64p), gp.ctypes.data_as(_f64p)))
+        return loss.value, dv, gp
+
     @property
     def handle(self):
         return self._h

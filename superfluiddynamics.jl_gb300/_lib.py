@@ -69,6 +69,8 @@ SIGNATURES = {
     "gpss_normalize": (ctypes.c_int, [_vp]),
     "gpss_ground_state": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                          ctypes.c_int, _f64p, _i64p]),
+    "gpss_adjoint": (ctypes.c_int, [_vp, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_double, _f64p, _f64p,
+                                    _f64p]),
     "gpss_sync": (ctypes.c_int, [_vp]),
     "gpss_event_record": (ctypes.c_int, [_vp, ctypes.c_int]),
     "gpss_event_elapsed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,

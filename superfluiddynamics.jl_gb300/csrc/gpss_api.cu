@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <new>
 #include "../../include/gpss.h"
 #include "gpss_internal.h"
@@ -327,15 +328,18 @@ template <typename T> static void set_finish(gpss_ctx *c, PassArgs<T> &a, int sl
 // prescale multiplies the first pass by the device scalar c->scale.
 template <typename T>
 static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl, int red_last,
-                         bool diag_kin, bool prescale, int fin_last = FIN_NONE)
+                         bool diag_kin, bool prescale, int fin_last = FIN_NONE, void *buf = nullptr,
+                         bool reverse = false)
 {
-    for (int axis = 0; axis < c->ndim; axis++) {
-        PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
+    void *field = buf ? buf : c->psi;
+    for (int step = 0; step < c->ndim; step++) {
+        const int axis = reverse ? c->ndim - 1 - step : step;
+        PassArgs<T> a = axis_args<T>(c, axis, field, field);
         const void *ph;
         GPSS_TRY(get_phase(c, axis, dtl, imag, 1, &ph, &a.prow));
         a.phase = (const vec2<T> *)ph;
-        if (prescale && axis == 0) a.scale = c->scale;
-        const bool last = axis == c->ndim - 1;
+        if (prescale && step == 0) a.scale = c->scale;
+        const bool last = step == c->ndim - 1;
         if (last && nl) {
             a.nl_mode = imag ? NL_IMAG : NL_REAL;
             a.V = c->have_V ? (const T *)c->V : nullptr;
@@ -553,6 +557,118 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
             GPSS_TRY(energy_impl<T>(c, diag->energy, &diag->mass));
         }
     }
+    return GPSS_OK;
+}
+
+// ---------------------------------------------------------------- adjoint --
+// device buffers of one gpss_adjoint call, released on every exit path
+struct DevBufs {
+    std::vector<void *> ptrs;
+    ~DevBufs()
+    {
+        for (void *p : ptrs) cudaFree(p);
+    }
+    int get(gpss_ctx *c, void **p, size_t bytes)
+    {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            return fail(c, GPSS_ENOMEM, "cudaMalloc(%zu) for the adjoint failed: %s", bytes, cudaGetErrorString(e));
+        }
+        ptrs.push_back(*p);
+        return GPSS_OK;
+    }
+};
+
+// one Strang step on `buf` as the forward of the adjoint: unmerged half
+// steps, no mass lock, so that the recomputed states are bitwise those of
+// the forward run
+template <typename T> static int strang_on(gpss_ctx *c, void *buf, double dt)
+{
+    GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, 0, false, false, FIN_NONE, buf));
+    return kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, 0, false, false, FIN_NONE, buf);
+}
+
+template <typename T>
+static int adjoint_impl(gpss_ctx *c, const double *psi_target, int nsteps, int K, double dt, double *loss,
+                        double *dLdV, double *dLdpsi0)
+{
+    using V = vec2<T>;
+    const size_t fb = (size_t)c->total * sizeof(V);
+    const int nck = (nsteps + K - 1) / K;
+    DevBufs m;
+    void *psi0, *ckpt, *states, *g, *tgt, *work, *dv, *red;
+    GPSS_TRY(m.get(c, &psi0, fb));
+    GPSS_TRY(m.get(c, &ckpt, fb * (size_t)nck));
+    GPSS_TRY(m.get(c, &states, fb * (size_t)K));
+    GPSS_TRY(m.get(c, &g, fb));
+    GPSS_TRY(m.get(c, &tgt, fb));
+    GPSS_TRY(m.get(c, &work, fb));
+    GPSS_TRY(m.get(c, &dv, (size_t)c->total * sizeof(double)));
+    GPSS_TRY(m.get(c, &red, sizeof(double) * (2 * 152 * 8 + 2)));
+    double *zdev = static_cast<double *>(red) + 2 * 152 * 8;
+    auto at = [&](void *base, int i) { return static_cast<void *>(static_cast<char *>(base) + fb * (size_t)i); };
+    const double dV = cell_volume(c);
+    CUDA_TRY(c, cudaMemcpyAsync(psi0, c->psi, fb, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(dv, 0, (size_t)c->total * sizeof(double), c->stream));
+    // target in the field precision
+    if (c->precision == GPSS_FP64) {
+        CUDA_TRY(c, cudaMemcpyAsync(tgt, psi_target, fb, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        CUDA_TRY(c, cudaMemcpyAsync(c->scratch, psi_target, (size_t)c->total * 16, cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, launch_f64_to_f32((const double *)c->scratch, (float *)tgt, 2 * c->total, c->stream));
+    }
+    // forward, keeping psi at the start of every segment
+    for (int s = 0; s < nsteps; s++) {
+        if (s % K == 0)
+            CUDA_TRY(c, cudaMemcpyAsync(at(ckpt, s / K), c->psi, fb, cudaMemcpyDeviceToDevice, c->stream));
+        GPSS_TRY(strang_on<T>(c, c->psi, dt));
+    }
+    // loss and the adjoint of the final field
+    CUDA_TRY(c, launch_overlap<T>((const V *)tgt, (const V *)c->psi, c->total, (double *)red, dV, zdev, c->stream));
+    double z[2];
+    CUDA_TRY(c, cudaMemcpyAsync(z, zdev, sizeof(z), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, launch_seed<T>((V *)g, (const V *)tgt, zdev, dV, c->total, c->stream));
+    c->launches += 3;
+    // backward, segment by segment from the last
+    const T *Vp = c->have_V ? (const T *)c->V : nullptr;
+    for (int seg = nck - 1; seg >= 0; seg--) {
+        const int start = seg * K, end = std::min(start + K, nsteps);
+        CUDA_TRY(c, cudaMemcpyAsync(work, at(ckpt, seg), fb, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(at(states, 0), work, fb, cudaMemcpyDeviceToDevice, c->stream));
+        for (int j = 1; j < end - start; j++) {
+            GPSS_TRY(strang_on<T>(c, work, dt));
+            CUDA_TRY(c, cudaMemcpyAsync(at(states, j), work, fb, cudaMemcpyDeviceToDevice, c->stream));
+        }
+        for (int nstep = end - 1; nstep >= start; nstep--) {
+            // second kinetic half step: g <- K^H g (conjugate phases, reverse axis order)
+            GPSS_TRY(kinetic_fused<T>(c, -dt * 0.5, 0, false, 0.0, 0, false, false, FIN_NONE, g, true));
+            // the state entering the nonlinear stage: K psi_n
+            CUDA_TRY(c, cudaMemcpyAsync(work, at(states, nstep - start), fb, cudaMemcpyDeviceToDevice, c->stream));
+            GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, 0, false, false, FIN_NONE, work));
+            CUDA_TRY(c, launch_nl_adjoint<T>((V *)g, (const V *)work, Vp, (double *)dv, c->beta, dt, c->total,
+                                             c->stream));
+            c->launches++;
+            // first kinetic half step
+            GPSS_TRY(kinetic_fused<T>(c, -dt * 0.5, 0, false, 0.0, 0, false, false, FIN_NONE, g, true));
+        }
+    }
+    // outputs; the context's field goes back to the initial state
+    if (dLdV) CUDA_TRY(c, cudaMemcpyAsync(dLdV, dv, (size_t)c->total * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (dLdpsi0) {
+        if (c->precision == GPSS_FP64) {
+            CUDA_TRY(c, cudaMemcpyAsync(dLdpsi0, g, fb, cudaMemcpyDeviceToHost, c->stream));
+        } else {
+            CUDA_TRY(c, launch_f32_to_f64((const float *)g, (double *)c->scratch, 2 * c->total, c->stream));
+            CUDA_TRY(c, cudaMemcpyAsync(dLdpsi0, c->scratch, (size_t)c->total * 16, cudaMemcpyDeviceToHost,
+                                        c->stream));
+        }
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c->psi, psi0, fb, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    *loss = 1.0 - (z[0] * z[0] + z[1] * z[1]);
+    if (!std::isfinite(*loss)) return fail(c, GPSS_ENONFINITE, "adjoint: non-finite loss");
     return GPSS_OK;
 }
 
@@ -854,6 +970,19 @@ int gpss_device_count(void)
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
     return n;
+}
+
+int gpss_adjoint(gpss_ctx *c, const double *psi_target, int nsteps, int K, double dt, double *loss,
+                 double *dLdV, double *dLdpsi0)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!psi_target || !loss) return fail(c, GPSS_EINVAL, "gpss_adjoint: null psi_target or loss");
+    if (nsteps < 1 || K < 1) return fail(c, GPSS_EINVAL, "gpss_adjoint: need nsteps >= 1 and K >= 1");
+    if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "dt must be finite");
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (c->precision == GPSS_FP32) return adjoint_impl<float>(c, psi_target, nsteps, K, dt, loss, dLdV, dLdpsi0);
+    return adjoint_impl<double>(c, psi_target, nsteps, K, dt, loss, dLdV, dLdpsi0);
 }
 
 int gpss_sync(gpss_ctx *c)

@@ -50,4 +50,16 @@ cudaError_t launch_nl(vec2<T> *psi, const T *V, double beta, double dt, int imag
                       cudaStream_t s);
 template <typename T>
 cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s);
+
+// discrete adjoint (adjoint.cu)
+// z[0..1] = dV * sum conj(a) b; partials needs 2 * 152 * 8 doubles
+template <typename T>
+cudaError_t launch_overlap(const vec2<T> *a, const vec2<T> *b, int64_t total, double *partials, double dV,
+                           double *z, cudaStream_t s);
+template <typename T>
+cudaError_t launch_seed(vec2<T> *g, const vec2<T> *target, const double *z, double dV, int64_t total,
+                        cudaStream_t s);
+template <typename T>
+cudaError_t launch_nl_adjoint(vec2<T> *g, const vec2<T> *psi_in, const T *V, double *dLdV, double beta, double dt,
+                              int64_t total, cudaStream_t s);
 }  // namespace gpss

@@ -75,7 +75,11 @@ template <> struct NLConst<float> {
     }
 };
 
-__device__ __forceinline__ double2 nl_apply(double2 v, double Vv, const NLConst<double> &c, bool imag)
+// The factor f = exp(-i theta) (real time) or exp(-theta) (imaginary time,
+// returned as (f, 0)) of one cell; the step is psi <- f psi (nl_rotate).  The
+// discrete adjoint recomputes the same factor, so forward and backward agree
+// to the bit.
+__device__ __forceinline__ double2 nl_factor(double2 v, double Vv, const NLConst<double> &c, bool imag)
 {
     const double rho = v.x * v.x + v.y * v.y;          // abs2
     const double r = Vv + c.beta * rho;
@@ -83,18 +87,28 @@ __device__ __forceinline__ double2 nl_apply(double2 v, double Vv, const NLConst<
         const double t = -r * c.dt;
         double s, co;
         sincos(t, &s, &co);
-        return make_double2(co * v.x - s * v.y, co * v.y + s * v.x);
+        return make_double2(co, s);
     }
-    const double f = exp(-r * c.dt);
-    return make_double2(f * v.x, f * v.y);
+    return make_double2(exp(-r * c.dt), 0.0);
 }
 
-__device__ __forceinline__ float2 nl_apply(float2 v, float Vv, const NLConst<float> &c, bool imag)
+template <typename V> __device__ __forceinline__ V nl_rotate(V f, V v)
+{
+    return mk<V>(f.x * v.x - f.y * v.y, f.x * v.y + f.y * v.x);
+}
+
+__device__ __forceinline__ double2 nl_apply(double2 v, double Vv, const NLConst<double> &c, bool imag)
+{
+    const double2 f = nl_factor(v, Vv, c, imag);
+    if (imag) return make_double2(f.x * v.x, f.x * v.y);
+    return nl_rotate(f, v);
+}
+
+__device__ __forceinline__ float2 nl_factor(float2 v, float Vv, const NLConst<float> &c, bool imag)
 {
     if (imag) {
         const float rho = fmaf(v.x, v.x, v.y * v.y);
-        const float f = expf(-fmaf(c.bf, rho, Vv) * c.df);
-        return make_float2(f * v.x, f * v.y);
+        return make_float2(expf(-fmaf(c.bf, rho, Vv) * c.df), 0.0f);
     }
     // rho = x^2 + y^2 in double-float
     DF px = two_prod(v.x, v.x), py = two_prod(v.y, v.y);
@@ -124,8 +138,14 @@ __device__ __forceinline__ float2 nl_apply(float2 v, float Vv, const NLConst<flo
     float ct = (quad & 1) ? sf : cf;
     if (quad == 1 || quad == 2) ct = -ct;
     if (quad >= 2) st = -st;
-    // psi * exp(-i theta)
-    return make_float2(ct * v.x + st * v.y, ct * v.y - st * v.x);
+    return make_float2(ct, -st);  // exp(-i theta)
+}
+
+__device__ __forceinline__ float2 nl_apply(float2 v, float Vv, const NLConst<float> &c, bool imag)
+{
+    const float2 f = nl_factor(v, Vv, c, imag);
+    if (imag) return make_float2(f.x * v.x, f.x * v.y);
+    return nl_rotate(f, v);
 }
 
 }  // namespace gpss

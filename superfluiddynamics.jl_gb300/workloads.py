@@ -15,6 +15,12 @@ cfg1  3D 256^3 on [0,2pi]^3, V = 0, rho = 1, xi = 0.05, c = 1:
 cfg2  3D 128^3 on [-10,10]^3, V = (x^2 + y^2 + 4 z^2)/2, beta = 2000, imaginary
       time; psi0 = unit-mass Gaussian + U(-1e-3, 1e-3) noise on re and im,
       renormalised; dt = 1e-3.
+cfg4  2D 256^2 on [-8,8]^2, trap V = (x^2+y^2)/2 plus a learnable V1 = 0,
+      g = 500, dt = 1e-3, 2000 steps, checkpoints every 50 steps; psi0 as
+      cfg0 (at 256^2); loss 1 - |<psi_target, psi(T)>|^2 with psi_target a
+      seeded vortex dipole: the psi0 envelope times tanh(r+/0.5) tanh(r-/0.5)
+      exp(i (atan2(y-y0, x-x0) - atan2(y-y0, x+x0))), vortices at (+-x0, y0),
+      x0 ~ U(1, 2), y0 ~ U(-0.5, 0.5); unit mass.
 """
 from __future__ import annotations
 
@@ -123,3 +129,18 @@ def cfg2(n=128, seed=0):
     V = np.asfortranarray(0.5 * (1 - 0.0) * (1.0 * X ** 2 + 1.0 * Y ** 2 + 4.0 * Z ** 2))
     return dict(name=f"cfg2-3d-{n}", shape=shape, bounds=bounds, psi=psi, V=V, coeffD=-0.5,
                 beta=2000.0, omega=0.0, dt=1e-3, nsteps=200, imag=True)
+
+
+def cfg4(n=256, seed=0):
+    """2D gradient workload: trap + learnable potential, vortex-dipole target."""
+    c = cfg0(n, seed)
+    rng = np.random.default_rng(4000 + seed)
+    X, Y = _mesh(c["shape"], c["bounds"])
+    x0, y0 = rng.uniform(1.0, 2.0), rng.uniform(-0.5, 0.5)
+    rp = np.hypot(X - x0, Y - y0)
+    rm = np.hypot(X + x0, Y - y0)
+    phase = np.arctan2(Y - y0, X - x0) - np.arctan2(Y - y0, X + x0)
+    env = np.exp(-(X ** 2 + Y ** 2) / 4.0)
+    tgt = env * np.tanh(rp / 0.5) * np.tanh(rm / 0.5) * np.exp(1j * phase)
+    c.update(name=f"cfg4-2d-{n}", target=np.asfortranarray(_unit_mass(tgt, c["bounds"])), nsteps=2000, K=50)
+    return c

@@ -1,0 +1,123 @@
+"""The discrete adjoint of the Strang step (gpss_adjoint) against central
+finite differences of the GPU's own FP64 forward map, and against the
+dual-number (forward-mode) restatement of the reference path in the oracle.
+
+Bar: the gradient agrees with finite differences to 1e-6 relative."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    return built_lib
+
+
+def _model(sfd, c, V, precision="fp64"):
+    g = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(g)
+    f.phi = c["psi"]
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=c["coeffD"], beta=c["beta"])
+    return f, sfd.NumModelSplit2(f, p, c["dt"], c["nsteps"], c["nsteps"], precision=precision,
+                                 merge=False, masslock=False)
+
+
+def _loss(sfd, O, c, V, nsteps, psi0=None):
+    """L of the GPU FP64 forward map (unmerged Strang, as in the adjoint)."""
+    cc = dict(c, psi=c["psi"] if psi0 is None else psi0)
+    f, n = _model(sfd, cc, V)
+    n.step(nsteps)
+    psi = f.phi.copy(order="F")
+    n.close()
+    dV = np.prod([(b[1] - b[0]) / m for m, b in zip(c["shape"], c["bounds"])])
+    z = np.sum(np.conj(c["target"]) * psi) * dV
+    return 1.0 - abs(z) ** 2
+
+
+def _directions(shape, count, seed, smooth=4.0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        a = rng.standard_normal(shape)
+        F = np.fft.fft2(a)
+        kx = np.fft.fftfreq(shape[0])[:, None] * shape[0]
+        ky = np.fft.fftfreq(shape[1])[None, :] * shape[1]
+        a = np.fft.ifft2(F * np.exp(-(kx ** 2 + ky ** 2) / smooth ** 2)).real
+        out.append(np.asfortranarray(a / np.max(np.abs(a))))
+    return out
+
+
+def test_adjoint_dV_vs_finite_differences(sfd, O, W):
+    """32 seeded directions, 32^2 copy of the gradient workload, 60 steps,
+    checkpoints every 7 steps (a partial last segment)."""
+    c = W.cfg4(32)
+    nsteps, K = 60, 7
+    f, n = _model(sfd, c, c["V"])
+    L, dLdV, _ = n.adjoint(c["target"], nsteps, K)
+    n.close()
+    eps = 1e-4
+    worst = 0.0
+    for dv in _directions(c["shape"], 32, seed=5):
+        fd = (_loss(sfd, O, c, c["V"] + eps * dv, nsteps) - _loss(sfd, O, c, c["V"] - eps * dv, nsteps)) / (2 * eps)
+        adj = float(np.sum(dLdV * dv))
+        worst = max(worst, abs(fd - adj) / max(abs(adj), 1e-300))
+    assert abs(L - _loss(sfd, O, c, c["V"], nsteps)) < 1e-13
+    assert worst < 1e-6
+
+
+def test_adjoint_dpsi0_vs_finite_differences(sfd, O, W):
+    c = W.cfg4(32)
+    nsteps, K = 40, 10
+    f, n = _model(sfd, c, c["V"])
+    L, _, g0 = n.adjoint(c["target"], nsteps, K)
+    n.close()
+    rng = np.random.default_rng(9)
+    eps = 1e-5
+    for _ in range(8):
+        d = rng.standard_normal(c["shape"]) + 1j * rng.standard_normal(c["shape"])
+        d = np.asfortranarray(d / np.max(np.abs(d)))
+        fd = (_loss(sfd, O, c, c["V"], nsteps, c["psi"] + eps * d)
+              - _loss(sfd, O, c, c["V"], nsteps, c["psi"] - eps * d)) / (2 * eps)
+        adj = float(np.real(np.sum(np.conj(g0) * d)))
+        assert abs(fd - adj) <= 1e-6 * abs(adj)
+
+
+def test_adjoint_vs_dual_numbers_of_the_reference_path(sfd, O, W):
+    """Directional derivative from the oracle's dual-number restatement of
+    the reference's Strang step on a 32^2 copy."""
+    c = W.cfg4(32)
+    nsteps, K = 50, 8
+    f, n = _model(sfd, c, c["V"])
+    L, dLdV, g0 = n.adjoint(c["target"], nsteps, K)
+    n.close()
+    rng = np.random.default_rng(3)
+    for dv in _directions(c["shape"], 4, seed=11):
+        dpsi = np.asfortranarray(0.1 * (rng.standard_normal(c["shape"]) + 1j * rng.standard_normal(c["shape"])))
+        Lo, dLo = O.np_tangent_loss(c["psi"], dpsi, c["V"], dv, c["target"], c["bounds"], coeffD=c["coeffD"],
+                                    beta=c["beta"], nsteps=nsteps, dt=c["dt"])
+        adj = float(np.sum(dLdV * dv)) + float(np.real(np.sum(np.conj(g0) * dpsi)))
+        assert abs(L - Lo) < 1e-12
+        assert abs(adj - dLo) <= 1e-8 * abs(dLo)
+
+
+def test_adjoint_cfg4_full_size(sfd, O, W):
+    """cfg4 at full size (256^2, 2000 steps, K = 50): FP64 gradient against
+    central differences on 4 of the seeded directions; FP32 forward with FP64
+    dL/dV accumulation against the FP64 gradient."""
+    c = W.cfg4(256)
+    nsteps, K = c["nsteps"], c["K"]
+    res = {}
+    for prec in ("fp64", "fp32"):
+        f, n = _model(sfd, c, c["V"], precision=prec)
+        res[prec] = n.adjoint(c["target"], nsteps, K)
+        n.close()
+    L64, dV64, g64 = res["fp64"]
+    L32, dV32, g32 = res["fp32"]
+    eps = 1e-4
+    for dv in _directions(c["shape"], 4, seed=21, smooth=16.0):
+        fd = (_loss(sfd, O, c, c["V"] + eps * dv, nsteps) - _loss(sfd, O, c, c["V"] - eps * dv, nsteps)) / (2 * eps)
+        adj = float(np.sum(dV64 * dv))
+        assert abs(fd - adj) <= 1e-6 * abs(adj)
+    assert abs(L32 - L64) < 1e-4
+    assert np.linalg.norm(dV32 - dV64) / np.linalg.norm(dV64) < 1e-2
