@@ -34,8 +34,9 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -58,6 +59,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     return ap.parse_args()
 
 
@@ -222,6 +224,30 @@ def run_reference(args, rank, world):
     return 0
 
 
+def measure_batch(sfd, W, calls=3):
+    """cfg3: 512 mixed-size 2D runs, 500 steps per call, one persistent launch
+    (CUDA graph) per call; host-timed around the synchronous call."""
+    c = W.cfg3()
+    runs = c["runs"]
+    b = sfd.BatchSplit2([r["n"] for r in runs], [r["bounds"] for r in runs], coeffD=c["coeffD"])
+    for i, r in enumerate(runs):
+        b.set_run(i, r["beta"], r["V"], r["psi"])
+    m0 = b.step(c["nsteps"], c["dt"])  # autotune + capture + one run
+    t = []
+    for _ in range(calls):
+        t0 = time.perf_counter()
+        m = b.step(c["nsteps"], c["dt"])
+        t.append(time.perf_counter() - t0)
+    tune = b.tuning()
+    b.close()
+    cells = sum(r["n"] * r["n"] for r in runs)
+    best = min(t)
+    return {"workload": "cfg3: 512 runs (256 x 64^2, 192 x 128^2, 64 x 256^2), 500 steps per call, FP32",
+            "value": cells * c["nsteps"] / best / 1e6, "unit": "Mcell-steps/s", "ms_per_call": best * 1e3,
+            "calls": calls, "runs": len(runs), "tuning": tune,
+            "max_rel_mass_drift": float(np.max(np.abs(m - m0) / m0))}
+
+
 # ----------------------------------------------------------------- GPU arm --
 def run_gpss(args, rank, world, local):
     import importlib
@@ -330,6 +356,11 @@ def run_gpss(args, rank, world, local):
         fp64 = {"value": v64, "unit": "Mcell-steps/s", "timesteps": k64,
                 "ms_per_timestep": ms64.value / k64, "fp32_fused_over_fp64_plain": value / world / v64}
 
+    # ---- batched runs (cfg3)
+    batch = None
+    if not args.no_batch:
+        batch = measure_batch(sfd, W)
+
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -368,6 +399,7 @@ def run_gpss(args, rank, world, local):
                      "whole_step_gbs": step_gbs},
         "cpu_baseline": cpu,
         "fp64_plain": fp64,
+        "batched": batch,
     }
     if clk:
         line["clocks"] = clk

@@ -142,6 +142,31 @@ int gpss_ground_state(gpss_ctx *ctx, double dt, double tol, int64_t max_steps, i
 int gpss_adjoint(gpss_ctx *ctx, const double *psi_target, int nsteps, int K, double dt, double *loss,
                  double *dLdV, double *dLdpsi0);
 
+/* ---- batched runs (an extension: the reference integrates one field at a time) ---- */
+
+typedef struct gpss_batch gpss_batch;
+
+/*
+ * A batch of nruns independent 2D real-time runs (NumModelSplit2 each), run
+ * r on an n[r] x n[r] grid (n[r] in {64, 128, 256}) over
+ * [lo[2r], hi[2r]) x [lo[2r+1], hi[2r+1]); coeffD shared.  FP32 fields,
+ * FP64 masses.  All runs advance together in one persistent kernel launch
+ * (captured in a CUDA graph) with a work queue; the first gpss_batch_step
+ * autotunes the launch policy on the batch itself.
+ */
+int gpss_batch_create(gpss_batch **out, int nruns, const int64_t *n, const double *lo, const double *hi,
+                      double coeffD);
+void gpss_batch_destroy(gpss_batch *b);
+const char *gpss_batch_last_error(const gpss_batch *b);
+/* beta, potential (real, n x n, x fastest; NULL = zero) and psi (interleaved complex) of one run */
+int gpss_batch_set_run(gpss_batch *b, int run, double beta, const double *V, const double *psi);
+/* nsteps Strang steps of dt for every run; mass_out[r] = sum |psi_r|^2 (no cell volume), nullable */
+int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out);
+int gpss_batch_download(gpss_batch *b, int run, double *psi);
+/* the autotuner's choice (policy 0: runs up to 128^2 in shared memory; 1: up to 64^2),
+ * queue order (0: largest first, 1: as given) and the four trial times in ms */
+int gpss_batch_tuning(const gpss_batch *b, int *policy, int *order, float *trial_ms);
+
 /* ---- timing and integration helpers (no reference counterpart) ---- */
 
 /* Make `device` the CUDA device that later gpss_create calls on this host

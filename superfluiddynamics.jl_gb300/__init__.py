@@ -38,7 +38,7 @@ from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_NOMASSLOCK, GPSS_F
 
 __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "PotentialZero",
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
-           "solve", "GPSSError", "version"]
+           "solve", "BatchSplit2", "GPSSError", "version"]
 
 _f64p = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -398,3 +398,72 @@ def solve(n: _SplitModel, istart: int = 1):
             for w in n.writers:
                 w(n.f, "res", it, n.dt)
     return res
+
+
+class BatchSplit2:
+    """Many independent 2D NumModelSplit2 runs (FP32 fields, FP64 masses)
+    advanced together by one persistent kernel launch (gpss_batch_*).
+
+    sizes: grid size n of each run (n x n, n in {64, 128, 256});
+    bounds: ((xmin, xmax), (ymin, ymax)) per run."""
+
+    def __init__(self, sizes, bounds, coeffD=-0.5):
+        L = _lib.lib()
+        self.sizes = [int(n) for n in sizes]
+        self.bounds = [tuple(tuple(float(v) for v in ax) for ax in b) for b in bounds]
+        nr = len(self.sizes)
+        n = (ctypes.c_int64 * nr)(*self.sizes)
+        lo = (ctypes.c_double * (2 * nr))(*[b[a][0] for b in self.bounds for a in range(2)])
+        hi = (ctypes.c_double * (2 * nr))(*[b[a][1] for b in self.bounds for a in range(2)])
+        h = ctypes.c_void_p()
+        rc = L.gpss_batch_create(ctypes.byref(h), nr, n, lo, hi, float(coeffD))
+        if rc != 0:
+            raise GPSSError(rc, "gpss_batch_create failed (sizes must be 64, 128 or 256; a GPU is needed)")
+        self._h = h
+
+    def _ck(self, rc):
+        if rc != 0:
+            msg = _lib.lib().gpss_batch_last_error(self._h)
+            raise GPSSError(rc, msg.decode() if msg else "")
+
+    def set_run(self, r, beta, V, psi):
+        n = self.sizes[r]
+        p = np.asfortranarray(np.asarray(psi, dtype=np.complex128))
+        if p.shape != (n, n):
+            raise ValueError("psi shape must be (n, n) of that run")
+        Vp = None
+        if V is not None:
+            Vp = np.asfortranarray(np.asarray(V, dtype=np.float64))
+            if Vp.shape != (n, n):
+                raise ValueError("V shape must be (n, n) of that run")
+        self._ck(_lib.lib().gpss_batch_set_run(self._h, int(r), float(beta),
+                                               None if Vp is None else Vp.ctypes.data_as(_f64p),
+                                               p.ctypes.data_as(_f64p)))
+
+    def step(self, nsteps, dt):
+        m = np.zeros(len(self.sizes), dtype=np.float64)
+        self._ck(_lib.lib().gpss_batch_step(self._h, int(nsteps), float(dt), m.ctypes.data_as(_f64p)))
+        return m
+
+    def download(self, r):
+        n = self.sizes[r]
+        out = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._ck(_lib.lib().gpss_batch_download(self._h, int(r), out.ctypes.data_as(_f64p)))
+        return out
+
+    def tuning(self):
+        pol, order = ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_float * 4)()
+        self._ck(_lib.lib().gpss_batch_tuning(self._h, ctypes.byref(pol), ctypes.byref(order), ms))
+        return {"policy": pol.value, "order": order.value, "trial_ms": list(ms)}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().gpss_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

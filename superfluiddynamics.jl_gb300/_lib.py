@@ -71,6 +71,14 @@ SIGNATURES = {
                                          ctypes.c_int, _f64p, _i64p]),
     "gpss_adjoint": (ctypes.c_int, [_vp, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_double, _f64p, _f64p,
                                     _f64p]),
+    "gpss_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double]),
+    "gpss_batch_destroy": (None, [_vp]),
+    "gpss_batch_last_error": (ctypes.c_char_p, [_vp]),
+    "gpss_batch_set_run": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _f64p, _f64p]),
+    "gpss_batch_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _f64p]),
+    "gpss_batch_download": (ctypes.c_int, [_vp, ctypes.c_int, _f64p]),
+    "gpss_batch_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_float)]),
     "gpss_sync": (ctypes.c_int, [_vp]),
     "gpss_event_record": (ctypes.c_int, [_vp, ctypes.c_int]),
     "gpss_event_elapsed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,

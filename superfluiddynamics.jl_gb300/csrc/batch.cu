@@ -1,0 +1,712 @@
+// batch.cu -- many independent 2D split-step runs of mixed sizes in one
+// persistent launch (an extension: the reference integrates one field at a
+// time; a batch is the workload of parameter sweeps).
+//
+// One CTA per SM (or several, see the policies below) pulls runs from an
+// atomic work queue, largest first, and integrates each run for all steps
+// before taking the next one:
+//
+//   * a run of n^2 <= 128^2 cells lives entirely in shared memory (psi and V,
+//     at most 192 KB): every pass of every step runs on chip and HBM sees
+//     the run twice (load, store);
+//   * a 256^2 run stays in global memory (L2-resident for a batch of this
+//     size): each pass walks its 16 tiles of 16 lines through a shared tile
+//     buffer with coalesced copies.
+//
+// A step is the merged real-time Strang sequence of the single-field path
+// (L(dt/2) N [L(dt) N]^(k-1) L(dt/2), passes x then y, the nonlinear flow
+// fused into the y pass) with the FP32 mass lock of that path (FP64 mass of
+// the run at the start of the call restored after each nonlinear stage).
+// FFT arithmetic is the same stage A/B/C decomposition with double-word
+// constants as pass_kernel.
+//
+// Policies (chosen by the autotuner in gpss_batch_step):
+//   policy 0  runs up to 128^2 in shared memory (204 KB per CTA, 1 CTA/SM)
+//   policy 1  only runs up to 64^2 in shared memory; 128^2 runs use tiles
+//             (72 KB per CTA, 3 CTAs/SM)
+// and the queue order (largest first, or as given).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <new>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "../../include/gpss.h"
+#include "gpss_internal.h"
+
+using namespace gpss;
+
+namespace {
+
+struct BatchRun {
+    int n;          // square grid n x n
+    int set;        // table set index
+    int64_t off;    // element offset of psi and V in the concatenated buffers
+    double beta;
+    int has_V;
+};
+
+struct TableSet {       // device pointers (float2), hi then lo halves
+    const float2 *tw;   // 4n: stage A, stage B
+    const float2 *phx[2];  // x phase for dt/2 and dt (2n each, 1/n included)
+    const float2 *phy[2];
+};
+
+struct BatchArgs {
+    const BatchRun *runs;
+    const TableSet *sets;
+    const int *order;
+    int nruns;
+    float2 *psi;
+    const float *V;
+    double *mass_out;
+    int *queue;
+    int *status;
+    int nsteps;
+    double dt;
+};
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double block_sum_double(float v, double *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = (double)v;
+    __syncthreads();
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < kThreads / 32; i++) s += red[i];
+    __syncthreads();
+    return s;
+}
+
+// One FFT -> phase -> iFFT pass over a tile of W lines held in shared memory,
+// in place.  XL: line w at base + w*N (contiguous); COL: position p of line w
+// at base + p*ps + w.  Optional nonlinear epilogue (V at the same positions)
+// and mass accumulation.
+template <int N, bool XL>
+__device__ __forceinline__ void tile_pass(float2 *base, int ps, const float2 *tw, const float2 *ph, bool scaled,
+                                          float scale, bool nl, const float *Vb, const NLConst<float> &nlc,
+                                          float &acc_mass)
+{
+    constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2, P = N2, W = kThreads / P;
+    const int tid = threadIdx.x;
+    const int w = XL ? tid / P : tid % W;
+    const int r = XL ? tid % P : tid / W;
+    auto raw = [&](int p) -> int { return XL ? w * N + p : p * ps + w; };
+    auto work = [&](int k1, int rr) -> int {
+        return XL ? w * N + k1 * N2 + (rr ^ (k1 & (N2 - 1))) : (k1 * N2 + rr) * ps + w;
+    };
+    const float2 *twA = tw, *twB = tw + 2 * N;
+    float2 v[N1];
+#pragma unroll
+    for (int j = 0; j < N1; j++) v[j] = base[raw(r + N2 * j)];
+    dft<N1, -1>(v);
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+        const int m = k1 * N2 + r;
+        base[work(k1, r)] = (k1 == 0 || r == 0) ? v[k1] : cmul2(v[k1], twA[m], twA[N + m]);
+    }
+    __syncthreads();
+    constexpr int NI = N1 / N2;
+#pragma unroll
+    for (int i = 0; i < NI; i++) {
+        const int k1 = r + P * i;
+        float2 u[N2];
+#pragma unroll
+        for (int rr = 0; rr < N2; rr++) u[rr] = base[work(k1, rr)];
+        dft<N2, -1>(u);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+            const int k = k1 + N1 * k2;
+            u[k2] = cmul2(u[k2], ph[k], ph[N + k]);
+            if (scaled) u[k2] = cscale(u[k2], scale);
+        }
+        dft<N2, +1>(u);
+#pragma unroll
+        for (int rr = 0; rr < N2; rr++) {
+            const int mb = rr * N1 + k1;
+            base[work(k1, rr)] = (k1 == 0 || rr == 0) ? u[rr] : cmulc2(u[rr], twB[mb], twB[N + mb]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) v[k1] = base[work(k1, r)];
+    dft<N1, +1>(v);
+    if (nl) {
+#pragma unroll
+        for (int j = 0; j < N1; j++) {
+            const float vv = Vb ? Vb[raw(r + N2 * j)] : 0.0f;
+            v[j] = nl_apply(v[j], vv, nlc, false);
+            acc_mass += v[j].x * v[j].x + v[j].y * v[j].y;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < N1; j++) base[raw(r + N2 * j)] = v[j];
+    __syncthreads();
+}
+
+template <int N> __device__ void load_tables(float2 *dst, const TableSet &ts)
+{
+    // tw 4N | phx(dt/2) 2N | phx(dt) 2N | phy(dt/2) 2N | phy(dt) 2N
+    for (int i = threadIdx.x; i < 4 * N; i += kThreads) dst[i] = ts.tw[i];
+    for (int i = threadIdx.x; i < 2 * N; i += kThreads) {
+        dst[4 * N + i] = ts.phx[0][i];
+        dst[6 * N + i] = ts.phx[1][i];
+        dst[8 * N + i] = ts.phy[0][i];
+        dst[10 * N + i] = ts.phy[1][i];
+    }
+}
+
+// the whole run in shared memory
+template <int N>
+__device__ void run_resident(const BatchArgs &A, const BatchRun &R, unsigned char *smem, double *red)
+{
+    constexpr int W = kThreads / Split<N>::N2;
+    float2 *psi = reinterpret_cast<float2 *>(smem);
+    float *Vs = reinterpret_cast<float *>(psi + N * N);
+    float2 *tab = reinterpret_cast<float2 *>(Vs + N * N);
+    const TableSet ts = A.sets[R.set];
+    load_tables<N>(tab, ts);
+    const float4 *gpsi = reinterpret_cast<const float4 *>(A.psi + R.off);
+    float4 *spsi = reinterpret_cast<float4 *>(psi);
+    for (int i = threadIdx.x; i < N * N / 2; i += kThreads) spsi[i] = gpsi[i];
+    if (R.has_V)
+        for (int i = threadIdx.x; i < N * N; i += kThreads) Vs[i] = A.V[R.off + i];
+    __syncthreads();
+    float m0 = 0.0f;
+    for (int i = threadIdx.x; i < N * N; i += kThreads) m0 += psi[i].x * psi[i].x + psi[i].y * psi[i].y;
+    const double mass0 = block_sum_double(m0, red);
+    const NLConst<float> nlc(R.beta, A.dt);
+    double scale = 1.0;
+    for (int s = 0; s <= A.nsteps; s++) {
+        const int full = (s > 0 && s < A.nsteps) ? 1 : 0;
+        const bool nl = s < A.nsteps;
+        const bool scaled = s > 0;
+        for (int t = 0; t < N / W; t++) {
+            float dummy = 0.0f;
+            tile_pass<N, true>(psi + t * W * N, 0, tab, tab + (full ? 6 : 4) * N, scaled, (float)scale, false,
+                               nullptr, nlc, dummy);
+        }
+        float acc = 0.0f;
+        for (int t = 0; t < N / W; t++)
+            tile_pass<N, false>(psi + t * W, N, tab, tab + (full ? 10 : 8) * N, false, 1.0f, nl,
+                                R.has_V ? Vs + t * W : nullptr, nlc, acc);
+        if (nl) {
+            const double m = block_sum_double(acc, red);
+            if (!(m > 0.0) || !isfinite(m)) {
+                if (threadIdx.x == 0) atomicOr(A.status, 1);
+                scale = 1.0;
+            } else {
+                scale = sqrt(mass0 / m);
+            }
+        }
+    }
+    float mf = 0.0f;
+    for (int i = threadIdx.x; i < N * N; i += kThreads) mf += psi[i].x * psi[i].x + psi[i].y * psi[i].y;
+    const double massf = block_sum_double(mf, red);
+    float4 *gout = reinterpret_cast<float4 *>(A.psi + R.off);
+    for (int i = threadIdx.x; i < N * N / 2; i += kThreads) gout[i] = spsi[i];
+    if (threadIdx.x == 0 && A.mass_out) A.mass_out[&R - A.runs] = massf;
+    __syncthreads();
+}
+
+// the run in global memory, tiles of W lines through a shared tile buffer
+template <int N>
+__device__ void run_tiled(const BatchArgs &A, const BatchRun &R, unsigned char *smem, double *red)
+{
+    constexpr int W = kThreads / Split<N>::N2;
+    float2 *tile = reinterpret_cast<float2 *>(smem);
+    float *Vt = reinterpret_cast<float *>(tile + W * N);
+    float2 *tab = reinterpret_cast<float2 *>(Vt + W * N);
+    const TableSet ts = A.sets[R.set];
+    load_tables<N>(tab, ts);
+    float2 *g = A.psi + R.off;
+    const float *gV = R.has_V ? A.V + R.off : nullptr;
+    __syncthreads();
+    float m0 = 0.0f;
+    for (int i = threadIdx.x; i < N * N; i += kThreads) {
+        const float2 q = g[i];
+        m0 += q.x * q.x + q.y * q.y;
+    }
+    const double mass0 = block_sum_double(m0, red);
+    const NLConst<float> nlc(R.beta, A.dt);
+    double scale = 1.0;
+    for (int s = 0; s <= A.nsteps; s++) {
+        const int full = (s > 0 && s < A.nsteps) ? 1 : 0;
+        const bool nl = s < A.nsteps;
+        const bool scaled = s > 0;
+        // x pass: tile t = rows t*W .. t*W+W-1, contiguous
+        for (int t = 0; t < N / W; t++) {
+            const float4 *src = reinterpret_cast<const float4 *>(g + (int64_t)t * W * N);
+            float4 *dst4 = reinterpret_cast<float4 *>(tile);
+            for (int i = threadIdx.x; i < W * N / 2; i += kThreads) dst4[i] = src[i];
+            __syncthreads();
+            float dummy = 0.0f;
+            tile_pass<N, true>(tile, 0, tab, tab + (full ? 6 : 4) * N, scaled, (float)scale, false, nullptr, nlc,
+                               dummy);
+            float4 *out = reinterpret_cast<float4 *>(g + (int64_t)t * W * N);
+            for (int i = threadIdx.x; i < W * N / 2; i += kThreads) out[i] = dst4[i];
+            __syncthreads();
+        }
+        // y pass: tile t = columns t*W .. t*W+W-1, position-major [p][w]
+        float acc = 0.0f;
+        for (int t = 0; t < N / W; t++) {
+            for (int i = threadIdx.x; i < W * N; i += kThreads) {
+                const int p = i / W, w = i % W;
+                tile[i] = g[(int64_t)p * N + t * W + w];
+                if (gV && nl) Vt[i] = gV[(int64_t)p * N + t * W + w];
+            }
+            __syncthreads();
+            tile_pass<N, false>(tile, W, tab, tab + (full ? 10 : 8) * N, false, 1.0f, nl, gV ? Vt : nullptr, nlc,
+                                acc);
+            for (int i = threadIdx.x; i < W * N; i += kThreads) {
+                const int p = i / W, w = i % W;
+                g[(int64_t)p * N + t * W + w] = tile[i];
+            }
+            __syncthreads();
+        }
+        if (nl) {
+            const double m = block_sum_double(acc, red);
+            if (!(m > 0.0) || !isfinite(m)) {
+                if (threadIdx.x == 0) atomicOr(A.status, 1);
+                scale = 1.0;
+            } else {
+                scale = sqrt(mass0 / m);
+            }
+        }
+    }
+    float mf = 0.0f;
+    for (int i = threadIdx.x; i < N * N; i += kThreads) {
+        const float2 q = g[i];
+        mf += q.x * q.x + q.y * q.y;
+    }
+    const double massf = block_sum_double(mf, red);
+    if (threadIdx.x == 0 && A.mass_out) A.mass_out[&R - A.runs] = massf;
+    __syncthreads();
+}
+
+template <int POLICY>
+__global__ void __launch_bounds__(kThreads, POLICY == 0 ? 1 : 3) batch_kernel(const BatchArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[kThreads / 32];
+    __shared__ int item;
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(A.queue, 1);
+        __syncthreads();
+        const int it = item;
+        __syncthreads();
+        if (it >= A.nruns) break;
+        const BatchRun &R = A.runs[A.order[it]];
+        if (R.n == 64) run_resident<64>(A, R, smem, red);
+        else if (R.n == 128) {
+            if (POLICY == 0) run_resident<128>(A, R, smem, red);
+            else run_tiled<128>(A, R, smem, red);
+        } else run_tiled<256>(A, R, smem, red);
+    }
+}
+
+// shared memory of a policy: the largest path it runs
+size_t policy_smem(int policy)
+{
+    auto resident = [](int n) { return (size_t)n * n * 8 + (size_t)n * n * 4 + (size_t)12 * n * 8; };
+    auto tiled = [](int n) {
+        const int W = kThreads / (n / 16);
+        return (size_t)W * n * 8 + (size_t)W * n * 4 + (size_t)12 * n * 8;
+    };
+    size_t s = std::max(resident(64), tiled(256));
+    if (policy == 0) s = std::max(s, resident(128));
+    else s = std::max(s, tiled(128));
+    return s;
+}
+
+}  // namespace
+
+struct gpss_batch {
+    int nruns = 0;
+    double coeffD = -0.5;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<BatchRun> runs;
+    std::vector<int> order_big, order_given;
+    std::vector<std::pair<int, std::pair<double, double>>> set_keys;  // (n, (Lx, Ly))
+    std::vector<std::pair<double, double>> boxes;                    // per run (Lx, Ly)
+    BatchRun *d_runs = nullptr;
+    TableSet *d_sets = nullptr;
+    int *d_order = nullptr;
+    float2 *d_psi = nullptr;
+    float *d_V = nullptr;
+    double *d_mass = nullptr;
+    int *d_queue = nullptr;
+    int *d_status = nullptr;
+    std::vector<void *> tables;
+    double tables_dt = NAN;
+    int64_t total = 0;
+    int policy = -1, order_mode = 0;  // tuned
+    float tuned_ms[4] = {0, 0, 0, 0};
+    cudaGraphExec_t graph = nullptr;
+    int graph_nsteps = -1;
+    double graph_dt = NAN;
+    std::string err;
+};
+
+static int bfail(gpss_batch *b, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (b) b->err = buf;
+    return code;
+}
+
+#define BTRY(b, call)                                                                              \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return bfail((b), GPSS_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+typedef long double ldouble;
+
+static void root_of_unity(int64_t k, int64_t n, ldouble *cs, ldouble *sn)
+{
+    const ldouble half_pi = 1.570796326794896619231321691639751442L;
+    k %= n;
+    if (k < 0) k += n;
+    const int64_t q = (4 * k) / n, r4 = 4 * k - q * n;
+    ldouble cc, ss;
+    if (2 * r4 <= n) {
+        const ldouble a = half_pi * (ldouble)r4 / (ldouble)n;
+        cc = cosl(a); ss = sinl(a);
+    } else {
+        const ldouble a = half_pi * (ldouble)(n - r4) / (ldouble)n;
+        cc = sinl(a); ss = cosl(a);
+    }
+    switch (q) {
+    case 0: *cs = cc; *sn = ss; break;
+    case 1: *cs = -ss; *sn = cc; break;
+    case 2: *cs = -cc; *sn = -ss; break;
+    default: *cs = ss; *sn = -cc; break;
+    }
+}
+
+// float2 hi[m] / lo[m] pairs from long-double values, rows of n
+static std::vector<float2> dw_table(const std::vector<ldouble> &re, const std::vector<ldouble> &im, int64_t n)
+{
+    const int64_t rows = (int64_t)re.size() / n;
+    std::vector<float2> out((size_t)(2 * n * rows));
+    for (int64_t r = 0; r < rows; r++)
+        for (int64_t k = 0; k < n; k++) {
+            const size_t i = (size_t)(r * n + k);
+            const float hr = (float)re[i], hi = (float)im[i];
+            out[(size_t)(r * 2 * n + k)] = make_float2(hr, hi);
+            out[(size_t)(r * 2 * n + n + k)] = make_float2((float)(re[i] - (ldouble)hr), (float)(im[i] - (ldouble)hi));
+        }
+    return out;
+}
+
+static int upload(gpss_batch *b, const std::vector<float2> &h, const float2 **dev)
+{
+    void *p = nullptr;
+    BTRY(b, cudaMalloc(&p, h.size() * sizeof(float2)));
+    b->tables.push_back(p);
+    BTRY(b, cudaMemcpy(p, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    *dev = static_cast<const float2 *>(p);
+    return GPSS_OK;
+}
+
+// twiddles and kinetic phase tables of every (n, box) in the batch for dt
+static int build_tables(gpss_batch *b, double dt)
+{
+    if (b->tables_dt == dt) return GPSS_OK;
+    BTRY(b, cudaStreamSynchronize(b->stream));
+    for (void *p : b->tables) cudaFree(p);
+    b->tables.clear();
+    std::vector<TableSet> sets(b->set_keys.size());
+    for (size_t si = 0; si < b->set_keys.size(); si++) {
+        const int64_t n = b->set_keys[si].first;
+        const int64_t N1 = n <= 16 ? n : 16, N2 = n / N1;
+        std::vector<ldouble> re((size_t)(2 * n)), im((size_t)(2 * n));
+        for (int64_t k1 = 0; k1 < N1; k1++)
+            for (int64_t r = 0; r < N2; r++) {
+                ldouble cs, sn;
+                root_of_unity(r * k1, n, &cs, &sn);
+                re[(size_t)(k1 * N2 + r)] = cs;
+                im[(size_t)(k1 * N2 + r)] = -sn;
+                re[(size_t)(n + r * N1 + k1)] = cs;
+                im[(size_t)(n + r * N1 + k1)] = -sn;
+            }
+        int rc = upload(b, dw_table(re, im, n), &sets[si].tw);
+        if (rc) return rc;
+        for (int axis = 0; axis < 2; axis++) {
+            const double L = axis == 0 ? b->set_keys[si].second.first : b->set_keys[si].second.second;
+            const double d = L / (double)n, mult = (6.283185307179586 / d) / (double)n;
+            for (int h = 0; h < 2; h++) {
+                const double dtl = h == 0 ? dt * 0.5 : dt;
+                std::vector<ldouble> pr((size_t)n), pi((size_t)n);
+                for (int64_t k = 0; k < n; k++) {
+                    const int64_t kk = k < (n + 1) / 2 ? k : k - n;
+                    const double xk = (double)kk * mult;
+                    const ldouble t = (ldouble)((b->coeffD * (xk * xk)) * dtl);
+                    pr[(size_t)k] = cosl(t) / (ldouble)n;
+                    pi[(size_t)k] = sinl(t) / (ldouble)n;
+                }
+                rc = upload(b, dw_table(pr, pi, n), axis == 0 ? &sets[si].phx[h] : &sets[si].phy[h]);
+                if (rc) return rc;
+            }
+        }
+    }
+    if (!b->d_sets) BTRY(b, cudaMalloc(&b->d_sets, sets.size() * sizeof(TableSet)));
+    BTRY(b, cudaMemcpy(b->d_sets, sets.data(), sets.size() * sizeof(TableSet), cudaMemcpyHostToDevice));
+    b->tables_dt = dt;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return GPSS_OK;
+}
+
+static cudaError_t launch_policy(gpss_batch *b, int policy, const BatchArgs &A)
+{
+    const size_t smem = policy_smem(policy);
+    int nsm = 0, per = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device);
+    if (e != cudaSuccess) return e;
+    if (policy == 0) {
+        e = cudaFuncSetAttribute(batch_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel<0>, kThreads, smem);
+    } else {
+        e = cudaFuncSetAttribute(batch_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel<1>, kThreads, smem);
+    }
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    int grid = std::min(nsm * per, b->nruns);
+    e = cudaMemsetAsync(A.queue, 0, sizeof(int), b->stream);
+    if (e != cudaSuccess) return e;
+    if (policy == 0) batch_kernel<0><<<grid, kThreads, smem, b->stream>>>(A);
+    else batch_kernel<1><<<grid, kThreads, smem, b->stream>>>(A);
+    return cudaGetLastError();
+}
+
+static BatchArgs make_args(gpss_batch *b, int nsteps, double dt, int order_mode)
+{
+    BatchArgs A;
+    A.runs = b->d_runs;
+    A.sets = b->d_sets;
+    A.order = b->d_order + (order_mode ? b->nruns : 0);
+    A.nruns = b->nruns;
+    A.psi = b->d_psi;
+    A.V = b->d_V;
+    A.mass_out = b->d_mass;
+    A.queue = b->d_queue;
+    A.status = b->d_status;
+    A.nsteps = nsteps;
+    A.dt = dt;
+    return A;
+}
+
+extern "C" {
+
+int gpss_batch_create(gpss_batch **out, int nruns, const int64_t *n, const double *lo, const double *hi, double coeffD)
+{
+    if (!out || !n || !lo || !hi || nruns < 1) return GPSS_EINVAL;
+    *out = nullptr;
+    gpss_batch *b = new (std::nothrow) gpss_batch();
+    if (!b) return GPSS_ENOMEM;
+    auto bail = [&](int rc) {
+        gpss_batch_destroy(b);
+        return rc;
+    };
+    b->nruns = nruns;
+    b->coeffD = coeffD;
+    b->runs.resize((size_t)nruns);
+    b->boxes.resize((size_t)nruns);
+    int64_t off = 0;
+    for (int r = 0; r < nruns; r++) {
+        if (n[r] != 64 && n[r] != 128 && n[r] != 256) return bail(GPSS_EINVAL);
+        const double Lx = hi[2 * r] - lo[2 * r], Ly = hi[2 * r + 1] - lo[2 * r + 1];
+        if (!(Lx > 0) || !(Ly > 0)) return bail(GPSS_EINVAL);
+        std::pair<int, std::pair<double, double>> key{(int)n[r], {Lx, Ly}};
+        int set = -1;
+        for (size_t i = 0; i < b->set_keys.size(); i++)
+            if (b->set_keys[i] == key) set = (int)i;
+        if (set < 0) {
+            set = (int)b->set_keys.size();
+            b->set_keys.push_back(key);
+        }
+        b->runs[(size_t)r] = BatchRun{(int)n[r], set, off, 1.0, 0};
+        off += n[r] * n[r];
+    }
+    b->total = off;
+    b->order_given.resize((size_t)nruns);
+    for (int r = 0; r < nruns; r++) b->order_given[(size_t)r] = r;
+    b->order_big = b->order_given;
+    std::stable_sort(b->order_big.begin(), b->order_big.end(),
+                     [&](int x, int y) { return b->runs[(size_t)x].n > b->runs[(size_t)y].n; });
+    if (cudaGetDevice(&b->device) != cudaSuccess) return bail(GPSS_ECUDA);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(GPSS_ECUDA);
+    if (cudaMalloc(&b->d_psi, (size_t)off * sizeof(float2)) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_V, (size_t)off * sizeof(float)) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_runs, (size_t)nruns * sizeof(BatchRun)) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_order, (size_t)nruns * 2 * sizeof(int)) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_mass, (size_t)nruns * sizeof(double)) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_queue, sizeof(int) * 2) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_status, sizeof(int) * 2) != cudaSuccess) return bail(GPSS_ENOMEM);
+    std::vector<int> orders(b->order_big);
+    orders.insert(orders.end(), b->order_given.begin(), b->order_given.end());
+    if (cudaMemcpy(b->d_order, orders.data(), orders.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(GPSS_ECUDA);
+    if (cudaMemset(b->d_V, 0, (size_t)off * sizeof(float)) != cudaSuccess) return bail(GPSS_ECUDA);
+    if (cudaMemset(b->d_psi, 0, (size_t)off * sizeof(float2)) != cudaSuccess) return bail(GPSS_ECUDA);
+    *out = b;
+    return GPSS_OK;
+}
+
+void gpss_batch_destroy(gpss_batch *b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void *p : b->tables) cudaFree(p);
+    void *ptrs[] = {b->d_runs, b->d_sets, b->d_order, b->d_psi, b->d_V, b->d_mass, b->d_queue, b->d_status};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char *gpss_batch_last_error(const gpss_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int gpss_batch_set_run(gpss_batch *b, int run, double beta, const double *V, const double *psi)
+{
+    if (!b) return GPSS_EINVAL;
+    if (run < 0 || run >= b->nruns || !psi || !std::isfinite(beta))
+        return bfail(b, GPSS_EINVAL, "gpss_batch_set_run: bad run index, psi or beta");
+    BTRY(b, cudaSetDevice(b->device));
+    BatchRun &R = b->runs[(size_t)run];
+    const int64_t cells = (int64_t)R.n * R.n;
+    std::vector<float> h((size_t)(2 * cells));
+    for (int64_t i = 0; i < 2 * cells; i++) h[(size_t)i] = (float)psi[i];
+    BTRY(b, cudaMemcpy(b->d_psi + R.off, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    R.beta = beta;
+    R.has_V = V != nullptr;
+    if (V) {
+        std::vector<float> hv((size_t)cells);
+        for (int64_t i = 0; i < cells; i++) hv[(size_t)i] = (float)V[i];
+        BTRY(b, cudaMemcpy(b->d_V + R.off, hv.data(), hv.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    BTRY(b, cudaMemcpy(b->d_runs + run, &R, sizeof(BatchRun), cudaMemcpyHostToDevice));
+    return GPSS_OK;
+}
+
+int gpss_batch_download(gpss_batch *b, int run, double *psi)
+{
+    if (!b) return GPSS_EINVAL;
+    if (run < 0 || run >= b->nruns || !psi) return bfail(b, GPSS_EINVAL, "gpss_batch_download: bad arguments");
+    BTRY(b, cudaSetDevice(b->device));
+    BTRY(b, cudaStreamSynchronize(b->stream));
+    const BatchRun &R = b->runs[(size_t)run];
+    const int64_t cells = (int64_t)R.n * R.n;
+    std::vector<float> h((size_t)(2 * cells));
+    BTRY(b, cudaMemcpy(h.data(), b->d_psi + R.off, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < 2 * cells; i++) psi[i] = h[(size_t)i];
+    return GPSS_OK;
+}
+
+int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out)
+{
+    if (!b) return GPSS_EINVAL;
+    if (nsteps < 1 || !std::isfinite(dt)) return bfail(b, GPSS_EINVAL, "gpss_batch_step: need nsteps >= 1, finite dt");
+    BTRY(b, cudaSetDevice(b->device));
+    int rc = build_tables(b, dt);
+    if (rc) return rc;
+    BTRY(b, cudaMemsetAsync(b->d_status, 0, sizeof(int), b->stream));
+    if (b->policy < 0) {
+        // autotune on this batch: each (policy, queue order) for a few steps on
+        // a copy-free trial (the runs are restored from a saved state)
+        void *save = nullptr;
+        BTRY(b, cudaMalloc(&save, (size_t)b->total * sizeof(float2)));
+        BTRY(b, cudaMemcpyAsync(save, b->d_psi, (size_t)b->total * sizeof(float2), cudaMemcpyDeviceToDevice, b->stream));
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        const int trial = std::min(nsteps, 8);
+        float best = 1e30f;
+        for (int cand = 0; cand < 4; cand++) {
+            const int policy = cand >> 1, order = cand & 1;
+            BatchArgs A = make_args(b, trial, dt, order);
+            cudaError_t e = launch_policy(b, policy, A);  // warm-up
+            if (e == cudaSuccess) {
+                cudaEventRecord(e0, b->stream);
+                e = launch_policy(b, policy, A);
+                cudaEventRecord(e1, b->stream);
+            }
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 1e30f;
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+            b->tuned_ms[cand] = ms;
+            if (ms < best) {
+                best = ms;
+                b->policy = policy;
+                b->order_mode = order;
+            }
+            cudaMemcpyAsync(b->d_psi, save, (size_t)b->total * sizeof(float2), cudaMemcpyDeviceToDevice, b->stream);
+        }
+        cudaStreamSynchronize(b->stream);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(save);
+        if (b->policy < 0) return bfail(b, GPSS_ECUDA, "autotune: no launch policy ran");
+    }
+    // one persistent launch, captured once per (nsteps, dt) in a CUDA graph
+    if (!b->graph || b->graph_nsteps != nsteps || b->graph_dt != dt) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        cudaGraph_t gr;
+        BTRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = launch_policy(b, b->policy, make_args(b, nsteps, dt, b->order_mode));
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &gr);
+        if (e != cudaSuccess) return bfail(b, GPSS_ECUDA, "batch capture: %s", cudaGetErrorString(e));
+        if (e2 != cudaSuccess) return bfail(b, GPSS_ECUDA, "batch capture: %s", cudaGetErrorString(e2));
+        e = cudaGraphInstantiate(&b->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return bfail(b, GPSS_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        b->graph_nsteps = nsteps;
+        b->graph_dt = dt;
+    }
+    BTRY(b, cudaGraphLaunch(b->graph, b->stream));
+    int st = 0;
+    BTRY(b, cudaMemcpyAsync(&st, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    if (mass_out)
+        BTRY(b, cudaMemcpyAsync(mass_out, b->d_mass, (size_t)b->nruns * sizeof(double), cudaMemcpyDeviceToHost,
+                                b->stream));
+    BTRY(b, cudaStreamSynchronize(b->stream));
+    if (st) return bfail(b, GPSS_ENONFINITE, "a run's mass became non-finite or zero");
+    return GPSS_OK;
+}
+
+int gpss_batch_tuning(const gpss_batch *b, int *policy, int *order, float *trial_ms)
+{
+    if (!b) return GPSS_EINVAL;
+    if (policy) *policy = b->policy;
+    if (order) *order = b->order_mode;
+    if (trial_ms)
+        for (int i = 0; i < 4; i++) trial_ms[i] = b->tuned_ms[i];
+    return GPSS_OK;
+}
+
+}  // extern "C"

@@ -15,6 +15,12 @@ cfg1  3D 256^3 on [0,2pi]^3, V = 0, rho = 1, xi = 0.05, c = 1:
 cfg2  3D 128^3 on [-10,10]^3, V = (x^2 + y^2 + 4 z^2)/2, beta = 2000, imaginary
       time; psi0 = unit-mass Gaussian + U(-1e-3, 1e-3) noise on re and im,
       renormalised; dt = 1e-3.
+cfg3  512 independent 2D runs: 256 x 64^2, 192 x 128^2, 64 x 256^2, all on
+      [-8,8]^2 (the box is this build's choice), V = (a x^2 + b y^2)/2 with
+      a, b ~ U(0.5, 2) plus 8 Gaussian bumps (heights U(0, 2), centres
+      U(-6, 6)^2, width 0.5), g ~ U(100, 1000), psi0 = the trap's oscillator
+      ground state times a cfg0-style phase imprint, unit mass; dt = 1e-3,
+      500 steps; FP32 fields, FP64 masses.
 cfg4  2D 256^2 on [-8,8]^2, trap V = (x^2+y^2)/2 plus a learnable V1 = 0,
       g = 500, dt = 1e-3, 2000 steps, checkpoints every 50 steps; psi0 as
       cfg0 (at 256^2); loss 1 - |<psi_target, psi(T)>|^2 with psi_target a
@@ -144,3 +150,33 @@ def cfg4(n=256, seed=0):
     tgt = env * np.tanh(rp / 0.5) * np.tanh(rm / 0.5) * np.exp(1j * phase)
     c.update(name=f"cfg4-2d-{n}", target=np.asfortranarray(_unit_mass(tgt, c["bounds"])), nsteps=2000, K=50)
     return c
+
+
+def cfg3_run(n, seed):
+    """One run of the batched workload (see cfg3)."""
+    shape = (n, n)
+    bounds = ((-8.0, 8.0), (-8.0, 8.0))
+    rng = np.random.default_rng(5000 + seed)
+    X, Y = _mesh(shape, bounds)
+    a, b = rng.uniform(0.5, 2.0, size=2)
+    V = 0.5 * (a * X ** 2 + b * Y ** 2)
+    for _ in range(8):
+        h = rng.uniform(0.0, 2.0)
+        cx, cy = rng.uniform(-6.0, 6.0, size=2)
+        V = V + h * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * 0.5 ** 2))
+    g = rng.uniform(100.0, 1000.0)
+    theta = _phase_field(rng, shape, bounds, 16, 3.0, 0.05)
+    psi = np.exp(-0.5 * (np.sqrt(a) * X ** 2 + np.sqrt(b) * Y ** 2)) * np.exp(1j * theta)
+    return dict(n=n, bounds=bounds, V=np.asfortranarray(V), beta=float(g),
+                psi=np.asfortranarray(_unit_mass(psi, bounds)))
+
+
+def cfg3(counts=(256, 192, 64), sizes=(64, 128, 256), seed=0):
+    """The batched workload: a list of runs (sizes mixed, seeded) and dt, steps."""
+    runs = []
+    k = 0
+    for cnt, n in zip(counts, sizes):
+        for _ in range(cnt):
+            runs.append(cfg3_run(n, seed * 100000 + k))
+            k += 1
+    return dict(name="cfg3-batch", runs=runs, coeffD=-0.5, dt=1e-3, nsteps=500)

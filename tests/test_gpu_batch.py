@@ -1,0 +1,54 @@
+"""Batched runs (gpss_batch_*): one persistent launch over runs of mixed
+sizes; every run against the single-field FP32 path and the FP64 oracle."""
+import numpy as np
+import pytest
+
+from helpers import run_model
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    return built_lib
+
+
+def test_batch_matches_single_runs_and_oracle(sfd, O, W):
+    runs = [W.cfg3_run(n, 77 + i) for i, n in enumerate((64, 128, 256, 64, 128, 256, 64))]
+    nsteps, dt = 40, 1e-3
+    b = sfd.BatchSplit2([r["n"] for r in runs], [r["bounds"] for r in runs])
+    for i, r in enumerate(runs):
+        b.set_run(i, r["beta"], r["V"], r["psi"])
+    masses = b.step(nsteps, dt)
+    tune = b.tuning()
+    assert tune["policy"] in (0, 1) and tune["order"] in (0, 1)
+    for i, r in enumerate(runs):
+        got = b.download(i)
+        single = run_model(sfd, (r["n"], r["n"]), r["bounds"], r["psi"], coeffD=-0.5, beta=r["beta"], V=r["V"],
+                           dt=dt, nsteps=nsteps, precision="fp32")
+        ref = O.c_step(r["psi"], r["bounds"], coeffD=-0.5, beta=r["beta"], V=r["V"], nsteps=nsteps, dt=dt)
+        assert O.rel_l2(got, single) < 5e-6  # two FP32 paths, mass sums ordered differently
+        assert O.rel_l2(got, ref) < 1e-5
+        m0 = np.sum(np.abs(r["psi"].astype(np.complex64)) ** 2)
+        assert abs(masses[i] - m0) / m0 < 1e-6
+    b.close()
+
+
+def test_batch_repeated_calls_are_consistent(sfd, O, W):
+    """Two calls of k steps equal one call of 2k steps up to FP32 round-off
+    (the graph is re-captured for a new step count)."""
+    runs = [W.cfg3_run(n, 300 + i) for i, n in enumerate((64, 128, 256))]
+    a = sfd.BatchSplit2([r["n"] for r in runs], [r["bounds"] for r in runs])
+    c = sfd.BatchSplit2([r["n"] for r in runs], [r["bounds"] for r in runs])
+    for i, r in enumerate(runs):
+        a.set_run(i, r["beta"], r["V"], r["psi"])
+        c.set_run(i, r["beta"], r["V"], r["psi"])
+    a.step(15, 1e-3)
+    a.step(15, 1e-3)
+    c.step(30, 1e-3)
+    for i, r in enumerate(runs):
+        ref = O.c_step(r["psi"], r["bounds"], coeffD=-0.5, beta=r["beta"], V=r["V"], nsteps=30, dt=1e-3)
+        assert O.rel_l2(a.download(i), ref) < 1e-5
+        assert O.rel_l2(c.download(i), ref) < 1e-5
+    a.close()
+    c.close()
