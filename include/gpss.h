@@ -43,8 +43,9 @@ extern "C" {
                                  leading half kinetic steps of consecutive steps */
 #define GPSS_FLAG_NOMASSLOCK 4 /* FP32 real time: do not restore the mass of the
                                  start of the call after each nonlinear stage */
-#define GPSS_FLAG_NOPIPE 8    /* fused passes without the asynchronous-copy pipeline
-                                 (same arithmetic, one tile per CTA) */
+#define GPSS_FLAG_PIPE 8      /* x passes through the persistent asynchronous-copy
+                                 pipeline (same arithmetic; the direct kernel is
+                                 faster on GB300 and is the default) */
 
 /* split schemes of gpss_step */
 #define GPSS_LIE 1            /* NumModelSplit1: L(dt) N(dt) */

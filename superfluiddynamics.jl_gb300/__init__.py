@@ -34,7 +34,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_NOMASSLOCK, GPSS_FLAG_NOMERGE,
-                   GPSS_FLAG_NOPIPE, GPSS_FLAG_PLAIN)
+                   GPSS_FLAG_PIPE, GPSS_FLAG_PLAIN)
 
 __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "PotentialZero",
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
@@ -204,7 +204,7 @@ class _SplitModel:
     scheme = 2
 
     def __init__(self, f: Field, param: GrossPitaevskiiParameters, dt, niter, freqbckp, *,
-                 precision="fp64", form="fused", merge=True, masslock=True, pipeline=True,
+                 precision="fp64", form="fused", merge=True, masslock=True, pipeline=False,
                  writers=()):
         if f._owner is not None:
             raise ValueError("this field already belongs to a model")
@@ -226,7 +226,7 @@ class _SplitModel:
         lo = (ctypes.c_double * 3)(*(list(g.min) + [0.0] * (3 - nd)))
         hi = (ctypes.c_double * 3)(*(list(g.max) + [1.0] * (3 - nd)))
         flags = ((GPSS_FLAG_PLAIN if form == "plain" else 0) | (0 if merge else GPSS_FLAG_NOMERGE)
-                 | (0 if masslock else GPSS_FLAG_NOMASSLOCK) | (0 if pipeline else GPSS_FLAG_NOPIPE))
+                 | (0 if masslock else GPSS_FLAG_NOMASSLOCK) | (GPSS_FLAG_PIPE if pipeline else 0))
         h = ctypes.c_void_p()
         _lib.check(L.gpss_create(ctypes.byref(h), nd, n, lo, hi, _PRECISION[precision], flags))
         self._h = h

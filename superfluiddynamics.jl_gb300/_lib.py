@@ -26,7 +26,7 @@ GPSS_FP32 = 32
 GPSS_FLAG_PLAIN = 1
 GPSS_FLAG_NOMERGE = 2
 GPSS_FLAG_NOMASSLOCK = 4
-GPSS_FLAG_NOPIPE = 8
+GPSS_FLAG_PIPE = 8
 GPSS_LIE = 1
 GPSS_STRANG = 2
 

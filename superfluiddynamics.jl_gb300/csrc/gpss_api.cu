@@ -267,14 +267,14 @@ template <typename T> static int blocks_for(gpss_ctx *c, int axis)
     return (int)((nl + W - 1) / W);
 }
 
-// Can the pipelined kernel run this fused pass?  Its tiles are 4096/n whole
-// lines; y tiles must not straddle z planes.  Only the x pass uses it: an x
-// tile is one contiguous bulk copy, while a y/z tile takes n row copies of
-// 128 bytes, which the copy engine moves about 3x slower than the direct
-// kernel's coalesced loads (measured at 256^3).
+// Does this fused pass go through the pipelined kernel?  Only on request
+// (GPSS_FLAG_PIPE) and only for x: an x tile is one contiguous bulk copy,
+// while a y/z tile takes n row copies of 128 bytes, which the copy engine
+// moves about 3x slower than coalesced loads; at 256^3 the direct kernel's x
+// pass is also 6% faster than the pipelined one (issue-bound, more warps).
 static bool pipe_ok(const gpss_ctx *c, int axis)
 {
-    if (c->flags & GPSS_FLAG_NOPIPE) return false;
+    if (!(c->flags & GPSS_FLAG_PIPE)) return false;
     if (axis != 0) return false;
     const int64_t n = c->n[axis];
     if (n != 64 && n != 128 && n != 256) return false;
@@ -709,7 +709,7 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if (ndim != 2 && ndim != 3) return fail(nullptr, GPSS_EINVAL, "ndim must be 2 or 3 (got %d)", ndim);
     if (precision != GPSS_FP64 && precision != GPSS_FP32)
         return fail(nullptr, GPSS_EINVAL, "precision must be GPSS_FP64 or GPSS_FP32 (got %d)", precision);
-    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_NOPIPE))
+    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_PIPE))
         return fail(nullptr, GPSS_EINVAL, "unknown flags 0x%x", flags);
     for (int a = 0; a < ndim; a++) {
         if (!is_pow2(n[a]) || n[a] < 2 || n[a] > 256)

@@ -101,6 +101,12 @@ template <typename T> struct PassArgs {
     const double *coord;     // coordinate of each row (rotation energy), nullable
 };
 
+// a double-word constant in shared memory: hi and lo adjacent, so one
+// 16-byte load (two for FP64) fetches both
+template <typename V> struct __align__(2 * sizeof(V)) DWord {
+    V hi, lo;
+};
+
 template <typename T> struct PassGeom {
     static constexpr int THREADS = 256;
 };
@@ -196,26 +202,29 @@ pass_kernel(const PassArgs<T> a)
     constexpr int N1 = S::N1, N2 = S::N2, P = S::P, W = S::W, LS = S::LS;
     constexpr int THREADS = S::THREADS;
 
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(32) unsigned char smem_raw[];
     V *sdata = reinterpret_cast<V *>(smem_raw);
-    V *stw = sdata + S::DATA;  // stage A: hi[N], lo[N]; stage B: hi[N], lo[N]
-    V *stwB = stw + 2 * N;
-    V *sph = stw + 4 * N;      // hi[N], lo[N]
+    DWord<V> *stw = reinterpret_cast<DWord<V> *>(sdata + S::DATA);  // stage A [N], stage B [N]
+    DWord<V> *stwB = stw + N;
+    DWord<V> *sph = stw + 2 * N;                                      // phase [N]
 
     const int tid = threadIdx.x;
-    // tables into shared memory
-    for (int i = tid; i < 4 * N; i += THREADS) stw[i] = a.tw[i];
-    if (MODE == MODE_FUSED && a.prow == 0)
-        for (int i = tid; i < 2 * N; i += THREADS) sph[i] = a.phase[i];
+    // tables into shared memory, hi/lo halves packed per entry
+    for (int i = tid; i < N; i += THREADS) {
+        stw[i] = DWord<V>{a.tw[i], a.tw[N + i]};
+        stwB[i] = DWord<V>{a.tw[2 * N + i], a.tw[3 * N + i]};
+        if (MODE == MODE_FUSED && a.prow == 0) sph[i] = DWord<V>{a.phase[i], a.phase[N + i]};
+    }
 
     const int w = XL ? tid / P : tid % W;
     const int r = XL ? tid % P : tid / W;
     const int g = blockIdx.x * W + w;
     const bool valid = g < a.nlines;
     const int gg = valid ? g : 0;
-    const int64_t base = (int64_t)(gg % a.m0) * a.s0 + (int64_t)(gg / a.m0) * a.s1;
+    // element indices fit 32 bits (at most 256^3 cells); x lines have unit stride
+    const uint32_t base = (uint32_t)((gg % a.m0) * a.s0 + (gg / a.m0) * a.s1);
     const int row = gg % a.rowmod;
-    const int64_t st = a.stride;
+    const uint32_t st = XL ? 1u : (uint32_t)a.stride;
 
     auto sidx = [&](int q) -> int {
         if constexpr (XL) return w * LS + q + q / N2;
@@ -233,7 +242,7 @@ pass_kernel(const PassArgs<T> a)
     if constexpr (MODE != MODE_INV) {
 #pragma unroll
         for (int j = 0; j < N1; j++) {
-            v[j] = valid ? a.in[base + (int64_t)(r + N2 * j) * st] : mk<V>((T)0, (T)0);
+            v[j] = a.in[base + (uint32_t)(r + N2 * j) * st];  // invalid threads read line 0
         }
         if constexpr (MODE == MODE_DIAG) {
             if (a.red & RED_POINT) {
@@ -242,7 +251,7 @@ pass_kernel(const PassArgs<T> a)
                     T rho = v[j].x * v[j].x + v[j].y * v[j].y;
                     acc_mass += rho;
                     acc_int += rho * rho;
-                    if (a.V && valid) acc_pot += a.V[base + (int64_t)(r + N2 * j) * st] * rho;
+                    if (a.V) acc_pot += a.V[base + (uint32_t)(r + N2 * j) * st] * rho;
                 }
             }
         }
@@ -268,9 +277,9 @@ pass_kernel(const PassArgs<T> a)
             }
 #pragma unroll
             for (int k = 0; k < N1; k++) {
-                const V ph = a.prow ? a.phase[row * a.prow + k] : sph[k];
-                const V pl = a.prow ? a.phase[row * a.prow + N + k] : sph[N + k];
-                v[k] = cmul2(v[k], ph, pl);
+                const DWord<V> p = a.prow ? DWord<V>{a.phase[row * a.prow + k], a.phase[row * a.prow + N + k]}
+                                          : sph[k];
+                v[k] = cmul2(v[k], p.hi, p.lo);
                 if (scaled) v[k] = cscale(v[k], scale);
             }
             dft<N1, +1>(v);
@@ -292,8 +301,7 @@ pass_kernel(const PassArgs<T> a)
             // spectrum out in natural order
         } else {  // MODE_INV
 #pragma unroll
-            for (int j = 0; j < N1; j++)
-                v[j] = valid ? a.in[base + (int64_t)j * st] : mk<V>((T)0, (T)0);
+            for (int j = 0; j < N1; j++) v[j] = a.in[base + (uint32_t)j * st];
             dft<N1, +1>(v);
 #pragma unroll
             for (int j = 0; j < N1; j++) v[j] = cscale(v[j], a.inv_n);
@@ -304,7 +312,11 @@ pass_kernel(const PassArgs<T> a)
 #pragma unroll
             for (int k1 = 0; k1 < N1; k1++) {
                 const int m = k1 * N2 + r;
-                V t = (k1 == 0 || r == 0) ? v[k1] : cmul2(v[k1], stw[m], stw[N + m]);
+                V t = v[k1];
+                if (k1 != 0 && r != 0) {
+                    const DWord<V> w2 = stw[m];
+                    t = cmul2(t, w2.hi, w2.lo);
+                }
                 sdata[sidx(m)] = t;
             }
             __syncthreads();
@@ -317,8 +329,7 @@ pass_kernel(const PassArgs<T> a)
             V u[N2];
             if constexpr (MODE == MODE_INV) {
 #pragma unroll
-                for (int k2 = 0; k2 < N2; k2++)
-                    u[k2] = valid ? a.in[base + (int64_t)(k1 + N1 * k2) * st] : mk<V>((T)0, (T)0);
+                for (int k2 = 0; k2 < N2; k2++) u[k2] = a.in[base + (uint32_t)(k1 + N1 * k2) * st];
             } else {
 #pragma unroll
                 for (int rr = 0; rr < N2; rr++) u[rr] = sdata[sidx(k1 * N2 + rr)];
@@ -327,7 +338,7 @@ pass_kernel(const PassArgs<T> a)
             if constexpr (MODE == MODE_FWD) {
                 if (valid) {
 #pragma unroll
-                    for (int k2 = 0; k2 < N2; k2++) a.out[base + (int64_t)(k1 + N1 * k2) * st] = u[k2];
+                    for (int k2 = 0; k2 < N2; k2++) a.out[base + (uint32_t)(k1 + N1 * k2) * st] = u[k2];
                 }
                 continue;
             }
@@ -352,17 +363,20 @@ pass_kernel(const PassArgs<T> a)
 #pragma unroll
                 for (int k2 = 0; k2 < N2; k2++) {
                     const int k = k1 + N1 * k2;
-                    const V ph = a.prow ? a.phase[row * a.prow + k] : sph[k];
-                    const V pl = a.prow ? a.phase[row * a.prow + N + k] : sph[N + k];
-                    u[k2] = cmul2(u[k2], ph, pl);
+                    const DWord<V> p = a.prow ? DWord<V>{a.phase[row * a.prow + k], a.phase[row * a.prow + N + k]}
+                                              : sph[k];
+                    u[k2] = cmul2(u[k2], p.hi, p.lo);
                     if (scaled) u[k2] = cscale(u[k2], scale);
                 }
             }
             dft<N2, +1>(u);  // u[rr] = Z[k1][rr]
 #pragma unroll
             for (int rr = 0; rr < N2; rr++) {
-                const int mb = rr * N1 + k1;
-                V t = (k1 == 0 || rr == 0) ? u[rr] : cmulc2(u[rr], stwB[mb], stwB[N + mb]);
+                V t = u[rr];
+                if (k1 != 0 && rr != 0) {
+                    const DWord<V> w2 = stwB[rr * N1 + k1];
+                    t = cmulc2(t, w2.hi, w2.lo);
+                }
                 sdata[sidx(k1 * N2 + rr)] = t;
             }
         }
@@ -387,7 +401,7 @@ pass_kernel(const PassArgs<T> a)
                 const bool imag = a.nl_mode == NL_IMAG;
 #pragma unroll
                 for (int j = 0; j < N1; j++) {
-                    const T vv = (a.V && valid) ? a.V[base + (int64_t)(r + N2 * j) * st] : (T)0;
+                    const T vv = a.V ? a.V[base + (uint32_t)(r + N2 * j) * st] : (T)0;
                     v[j] = nl_apply(v[j], vv, nlc, imag);
                 }
             }
@@ -397,7 +411,7 @@ pass_kernel(const PassArgs<T> a)
                     const T rho = v[j].x * v[j].x + v[j].y * v[j].y;
                     acc_mass += rho;
                     acc_int += rho * rho;
-                    if (a.V && valid) acc_pot += a.V[base + (int64_t)(r + N2 * j) * st] * rho;
+                    if (a.V) acc_pot += a.V[base + (uint32_t)(r + N2 * j) * st] * rho;
                 }
             } else if (a.red & RED_MASS) {
 #pragma unroll
@@ -406,12 +420,12 @@ pass_kernel(const PassArgs<T> a)
         }
         if (valid) {
 #pragma unroll
-            for (int j = 0; j < N1; j++) a.out[base + (int64_t)(r + N2 * j) * st] = v[j];
+            for (int j = 0; j < N1; j++) a.out[base + (uint32_t)(r + N2 * j) * st] = v[j];
         }
     } else if constexpr (MODE == MODE_FWD && N2 == 1) {
         if (valid) {
 #pragma unroll
-            for (int k = 0; k < N1; k++) a.out[base + (int64_t)k * st] = v[k];
+            for (int k = 0; k < N1; k++) a.out[base + (uint32_t)k * st] = v[k];
         }
     }
 

@@ -5,7 +5,7 @@ import numpy as np
 
 def run_model(sfd, shape, bounds, psi0, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, dt=1e-3,
               nsteps=1, scheme=2, imag=False, precision="fp64", form="fused", merge=True,
-              per_call=None, masslock=True, pipeline=True):
+              per_call=None, masslock=True, pipeline=False):
     g = sfd.Grid(shape, bounds)
     f = sfd.Field(g)
     f.phi = psi0
