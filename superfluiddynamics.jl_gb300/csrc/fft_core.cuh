@@ -25,6 +25,38 @@ template <typename V> __device__ __forceinline__ V mk(decltype(V::x) x, decltype
 }
 template <typename V> __device__ __forceinline__ V cadd(V a, V b) { return mk<V>(a.x + b.x, a.y + b.y); }
 template <typename V> __device__ __forceinline__ V csub(V a, V b) { return mk<V>(a.x - b.x, a.y - b.y); }
+// FP32: a complex add or subtract is one packed f32x2 instruction (sm_100
+// and later), with the same round-to-nearest result per component as two
+// scalar operations.
+#ifndef GPSS_PACKED_F32
+#define GPSS_PACKED_F32 1
+#endif
+#if GPSS_PACKED_F32
+__device__ __forceinline__ unsigned long long pack_f2(float2 a)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 unpack_f2(unsigned long long r)
+{
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pack_f2(a)), "l"(pack_f2(b)));
+    return unpack_f2(d);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pack_f2(a)), "l"(pack_f2(b)));
+    return unpack_f2(d);
+}
+#endif
 // a * b
 template <typename V> __device__ __forceinline__ V cmul(V a, V b)
 {
@@ -122,11 +154,18 @@ template <int DIR, typename V> __device__ __forceinline__ void dft2(V &a0, V &a1
 template <int DIR, typename V> __device__ __forceinline__ void dft4(V &a0, V &a1, V &a2, V &a3)
 {
     V s02 = cadd(a0, a2), d02 = csub(a0, a2);
-    V s13 = cadd(a1, a3), d13 = mul_i<DIR>(csub(a1, a3));
+    V s13 = cadd(a1, a3), t = csub(a1, a3);
     a0 = cadd(s02, s13);
     a2 = csub(s02, s13);
-    a1 = cadd(d02, d13);
-    a3 = csub(d02, d13);
+    // a1 = d02 + DIR i t, a3 = d02 - DIR i t, written per component (the
+    // swap of re/im is free here, but not inside a packed FP32 operation)
+    if (DIR < 0) {
+        a1 = mk<V>(d02.x + t.y, d02.y - t.x);
+        a3 = mk<V>(d02.x - t.y, d02.y + t.x);
+    } else {
+        a1 = mk<V>(d02.x - t.y, d02.y + t.x);
+        a3 = mk<V>(d02.x + t.y, d02.y - t.x);
+    }
 }
 
 // In-place natural-order DFT of size N (1, 2, 4, 8, 16) on a[0..N).

@@ -14,6 +14,7 @@
 // from their Taylor series (degree 9 and 10: truncation below 3e-9 relative
 // on |f| <= pi/4, under half an FP32 ulp) and the quadrant.  The error of the
 // reduced argument is about one float ulp of f, whatever the size of theta.
+// Cells with |theta| <= 0.78 take a short path without reduction (below).
 #pragma once
 #include <cuda_runtime.h>
 #include "fft_core.cuh"
@@ -66,14 +67,44 @@ template <> struct NLConst<double> {
     __device__ __forceinline__ NLConst(double b, double d) : beta(b), dt(d) {}
 };
 template <> struct NLConst<float> {
-    float bh, bl, dh, dl, bf, df;
+    float bh, bl, dh, dl, bf, df, bdh, bdl;
     __device__ __forceinline__ NLConst(double b, double d)
     {
         bh = (float)b; bl = (float)(b - (double)bh);
         dh = (float)d; dl = (float)(d - (double)dh);
         bf = bh; df = dh;
+        const double bd = b * d;
+        bdh = (float)bd; bdl = (float)(bd - (double)bdh);
     }
 };
+
+// Short path of the FP32 real-time factor, taken by every cell whose
+// |theta| <= NL_SHORT_MAX < pi/4 (no reduction needed): theta from one-float
+// rho with the constants beta*dt and dt kept as float pairs, so that their
+// rounding adds no systematic phase drift; the error of theta is a few float
+// ulps of theta itself, below 2e-7 absolute.
+#define NL_SHORT_MAX 0.78f
+__device__ __forceinline__ float nl_theta_short(float2 v, float Vv, const NLConst<float> &c)
+{
+    const float rho = fmaf(v.x, v.x, v.y * v.y);
+    float th = fmaf(rho, c.bdh, rho * c.bdl);
+    if (Vv != 0.0f) th = fmaf(Vv, c.dh, fmaf(Vv, c.dl, th));
+    return th;
+}
+__device__ __forceinline__ float2 nl_factor_short(float th)
+{
+    float sf, cf;
+    sincos_reduced(th, &sf, &cf);
+    return make_float2(cf, -sf);
+}
+// True when every cell with |psi|^2 <= rmax and |V| <= vmax takes the short
+// path (a bound on |nl_theta_short| with a margin far above its rounding), so
+// a warp that agrees on it may call nl_factor_short directly and still
+// produce exactly what nl_factor gives cell by cell.
+__device__ __forceinline__ bool nl_short_bound(float rmax, float vmax, const NLConst<float> &c)
+{
+    return (fabsf(c.bdh) * rmax + fabsf(c.dh) * vmax) * 1.001f <= NL_SHORT_MAX;
+}
 
 // The factor f = exp(-i theta) (real time) or exp(-theta) (imaginary time,
 // returned as (f, 0)) of one cell; the step is psi <- f psi (nl_rotate).  The
@@ -109,6 +140,10 @@ __device__ __forceinline__ float2 nl_factor(float2 v, float Vv, const NLConst<fl
     if (imag) {
         const float rho = fmaf(v.x, v.x, v.y * v.y);
         return make_float2(expf(-fmaf(c.bf, rho, Vv) * c.df), 0.0f);
+    }
+    {
+        const float th = nl_theta_short(v, Vv, c);
+        if (fabsf(th) <= NL_SHORT_MAX) return nl_factor_short(th);
     }
     // rho = x^2 + y^2 in double-float
     DF px = two_prod(v.x, v.x), py = two_prod(v.y, v.y);

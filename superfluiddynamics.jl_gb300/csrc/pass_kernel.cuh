@@ -107,8 +107,16 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
     V hi, lo;
 };
 
+// resident CTAs per SM that the FP32 kernels are compiled for.  3 (at most 80
+// registers) measured best at 256^3: 4 (64 registers) spills and runs 15-25%
+// slower, no bound lets the fused kernels grow past 85 registers (2 CTAs per
+// SM) and run 1.7x slower.
+#ifndef GPSS_PASS_MIN_BLOCKS_F32
+#define GPSS_PASS_MIN_BLOCKS_F32 3
+#endif
 template <typename T> struct PassGeom {
     static constexpr int THREADS = 256;
+    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? GPSS_PASS_MIN_BLOCKS_F32 : 1;
 };
 
 template <int N> struct Split {
@@ -149,6 +157,33 @@ __device__ __forceinline__ void block_sum_store(T v, double *partials, int q, T 
 // The last CTA of the grid to finish sums every CTA's partials (same fixed
 // order whichever CTA is last, so results are deterministic), writes the
 // sums and the next-pass factor, and re-arms the counter for the next launch.
+// CTA sums of the quantities in qmask (vals[q], q < RQ_COUNT) with one
+// barrier; thread 0 writes partials[q * gridDim.x + blockIdx.x]
+template <typename T, int THREADS>
+__device__ __forceinline__ void block_sums_store(const T (&vals)[RQ_COUNT], unsigned qmask, double *partials)
+{
+    __shared__ T red_smem[RQ_COUNT][THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < RQ_COUNT; q++) {
+        if (!(qmask & (1u << q))) continue;
+        T v = vals[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red_smem[q][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < RQ_COUNT; q++) {
+            if (!(qmask & (1u << q))) continue;
+            double s = 0.0;
+#pragma unroll
+            for (int i = 0; i < THREADS / 32; i++) s += (double)red_smem[q][i];
+            partials[(size_t)q * gridDim.x + blockIdx.x] = s;
+        }
+    }
+}
+
 template <typename T, int THREADS>
 __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned qmask)
 {
@@ -194,7 +229,7 @@ __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned 
 }
 
 template <typename T, int N, bool XL, int MODE>
-__global__ void __launch_bounds__(PassGeom<T>::THREADS)
+__global__ void __launch_bounds__(PassGeom<T>::THREADS, PassGeom<T>::MIN_BLOCKS)
 pass_kernel(const PassArgs<T> a)
 {
     using V = vec2<T>;
@@ -218,12 +253,6 @@ pass_kernel(const PassArgs<T> a)
 
     const int w = XL ? tid / P : tid % W;
     const int r = XL ? tid % P : tid / W;
-    const int g = blockIdx.x * W + w;
-    const bool valid = g < a.nlines;
-    const int gg = valid ? g : 0;
-    // element indices fit 32 bits (at most 256^3 cells); x lines have unit stride
-    const uint32_t base = (uint32_t)((gg % a.m0) * a.s0 + (gg / a.m0) * a.s1);
-    const int row = gg % a.rowmod;
     const uint32_t st = XL ? 1u : (uint32_t)a.stride;
 
     auto sidx = [&](int q) -> int {
@@ -238,11 +267,28 @@ pass_kernel(const PassArgs<T> a)
     // accumulators (precision of the field; the CTA totals are kept in FP64)
     T acc_mass = 0, acc_pot = 0, acc_int = 0, acc_kin = 0, acc_rot = 0;
 
+    // tiles of W lines; a grid smaller than the tile count loops (the tables
+    // and the reduction tail are then paid once per CTA, not once per tile)
+    const int ntiles = (a.nlines + W - 1) / W;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int g = tile * W + w;
+    const bool valid = g < a.nlines;
+    const int gg = valid ? g : 0;
+    // element indices fit 32 bits (at most 256^3 cells); x lines have unit stride
+    const uint32_t base = (uint32_t)((gg % a.m0) * a.s0 + (gg / a.m0) * a.s1);
+    const int row = gg % a.rowmod;
+
     V v[N1];
     if constexpr (MODE != MODE_INV) {
 #pragma unroll
         for (int j = 0; j < N1; j++) {
-            v[j] = a.in[base + (uint32_t)(r + N2 * j) * st];  // invalid threads read line 0
+            v[j] = a.in[base + (uint32_t)(r + N2 * j) * st];  // invalid threads read line 0 ...
+        }
+        if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
+            if (!valid) {  // ... and sum nothing
+#pragma unroll
+                for (int j = 0; j < N1; j++) v[j] = mk<V>((T)0, (T)0);
+            }
         }
         if constexpr (MODE == MODE_DIAG) {
             if (a.red & RED_POINT) {
@@ -257,7 +303,7 @@ pass_kernel(const PassArgs<T> a)
         }
         dft<N1, -1>(v);
     }
-    __syncthreads();  // tables ready
+    __syncthreads();  // tables ready; the previous tile's stage C is done with sdata
 
     if constexpr (N2 == 1) {
         // the whole line lives in this thread: v[k] = X[k]
@@ -399,10 +445,41 @@ pass_kernel(const PassArgs<T> a)
             if (a.nl_mode != NL_NONE) {
                 const NLConst<T> nlc(a.nl_beta, a.nl_dt);
                 const bool imag = a.nl_mode == NL_IMAG;
+                bool done = false;
+                if constexpr (sizeof(T) == 4) {
+                    if (!imag) {
+                        // one vote per warp: if every cell of the warp takes the
+                        // short path, skip the per-cell choice
+                        T rmax = 0, vmax = 0;
 #pragma unroll
-                for (int j = 0; j < N1; j++) {
-                    const T vv = a.V ? a.V[base + (uint32_t)(r + N2 * j) * st] : (T)0;
-                    v[j] = nl_apply(v[j], vv, nlc, imag);
+                        for (int j = 0; j < N1; j++) rmax = fmaxf(rmax, fmaf(v[j].x, v[j].x, v[j].y * v[j].y));
+                        if (a.V) {
+#pragma unroll
+                            for (int j = 0; j < N1; j++)
+                                vmax = fmaxf(vmax, fabsf(a.V[base + (uint32_t)(r + N2 * j) * st]));
+                        }
+                        if (__all_sync(0xffffffffu, nl_short_bound(rmax, vmax, nlc))) {
+                            if (a.V) {
+#pragma unroll
+                                for (int j = 0; j < N1; j++) {
+                                    const T vv = a.V[base + (uint32_t)(r + N2 * j) * st];
+                                    v[j] = nl_rotate(nl_factor_short(nl_theta_short(v[j], vv, nlc)), v[j]);
+                                }
+                            } else {
+#pragma unroll
+                                for (int j = 0; j < N1; j++)
+                                    v[j] = nl_rotate(nl_factor_short(nl_theta_short(v[j], (T)0, nlc)), v[j]);
+                            }
+                            done = true;
+                        }
+                    }
+                }
+                if (!done) {
+#pragma unroll
+                    for (int j = 0; j < N1; j++) {
+                        const T vv = a.V ? a.V[base + (uint32_t)(r + N2 * j) * st] : (T)0;
+                        v[j] = nl_apply(v[j], vv, nlc, imag);
+                    }
                 }
             }
             if (a.red & RED_POINT) {
@@ -429,24 +506,16 @@ pass_kernel(const PassArgs<T> a)
         }
     }
 
+    }  // tiles
+
     if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
         if (a.red) {
-            __shared__ T red_smem[THREADS / 32];
-            if (!valid) { acc_mass = acc_pot = acc_int = acc_kin = acc_rot = 0; }
-            if (a.red & (RED_POINT | RED_MASS))
-                block_sum_store<T, THREADS>(acc_mass, a.partials, RQ_MASS, red_smem);
-            if (a.red & RED_POINT) {
-                block_sum_store<T, THREADS>(acc_pot, a.partials, RQ_POT, red_smem);
-                block_sum_store<T, THREADS>(acc_int, a.partials, RQ_INT, red_smem);
-            }
-            if (a.red & RED_KIN) {
-                block_sum_store<T, THREADS>(acc_kin, a.partials, RQ_KIN, red_smem);
-                block_sum_store<T, THREADS>(acc_rot, a.partials, RQ_ROT, red_smem);
-            }
             unsigned qmask = 0;
             if (a.red & (RED_POINT | RED_MASS)) qmask |= 1u << RQ_MASS;
             if (a.red & RED_POINT) qmask |= (1u << RQ_POT) | (1u << RQ_INT);
             if (a.red & RED_KIN) qmask |= (1u << RQ_KIN) | (1u << RQ_ROT);
+            const T vals[RQ_COUNT] = {acc_mass, acc_pot, acc_int, acc_kin, acc_rot};
+            block_sums_store<T, THREADS>(vals, qmask, a.partials);
             finish_reduction<T, THREADS>(a, qmask);
         }
     }
