@@ -44,7 +44,7 @@ struct gpss_ctx {
     double *partials = nullptr;
     int max_blocks = 0;
     double *sums = nullptr;   // [4][RQ_COUNT]: slots 0..2 per axis, slot 3 diagnostics
-    double *scale = nullptr;  // [1]
+    double *scale = nullptr;  // ScaleCell: the factor in FP64 and as a float
     int *status = nullptr;    // [1]
     unsigned int *counter = nullptr;  // arrival counter of the in-kernel reduction finish
     std::vector<PhaseEntry> phases;
@@ -345,6 +345,7 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
             a.V = c->have_V ? (const T *)c->V : nullptr;
             a.nl_beta = c->beta;
             a.nl_dt = dtnl;
+            a.nl_split = nl_split(c->beta, dtnl);
         }
         if (last) a.red |= red_last;
         if (a.red & RED_POINT) a.V = c->have_V ? (const T *)c->V : nullptr;
@@ -782,8 +783,8 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if ((rc = dev_alloc(c, (void **)&c->counter, sizeof(unsigned int) * 2))) return bail(rc);
     e = cudaMemset(c->counter, 0, sizeof(unsigned int) * 2);
     if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemset: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
-    double one = 1.0;
-    e = cudaMemcpy(c->scale, &one, sizeof(double), cudaMemcpyHostToDevice);
+    const ScaleCell one = {1.0, 1.0f};
+    e = cudaMemcpy(c->scale, &one, sizeof(one), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
     *out = c;
     return GPSS_OK;
@@ -1035,6 +1036,7 @@ int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double 
             a.V = c->have_V ? (const T *)c->V : nullptr;
             a.nl_beta = c->beta;
             a.nl_dt = dt;
+            a.nl_split = nl_split(c->beta, dt);
         }
         GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));  // warm-up
         CUDA_TRY(c, cudaEventRecord(c->ev[6], c->stream));

@@ -66,17 +66,38 @@ template <> struct NLConst<double> {
     double beta, dt;
     __device__ __forceinline__ NLConst(double b, double d) : beta(b), dt(d) {}
 };
+// beta, dt and beta*dt as float pairs hi + lo.  Formed on the host for the
+// pass kernels: GB300 executes FP64 at a small fraction of its FP32 rate, and
+// a dozen FP64 operations per thread took a quarter of the FP64 pipe in a
+// 256^3 pass.
+struct NLSplit {
+    float bh, bl, dh, dl, bdh, bdl;
+};
+__host__ __device__ inline NLSplit nl_split(double b, double d)
+{
+    NLSplit s;
+    s.bh = (float)b; s.bl = (float)(b - (double)s.bh);
+    s.dh = (float)d; s.dl = (float)(d - (double)s.dh);
+    const double bd = b * d;
+    s.bdh = (float)bd; s.bdl = (float)(bd - (double)s.bdh);
+    return s;
+}
 template <> struct NLConst<float> {
     float bh, bl, dh, dl, bf, df, bdh, bdl;
-    __device__ __forceinline__ NLConst(double b, double d)
-    {
-        bh = (float)b; bl = (float)(b - (double)bh);
-        dh = (float)d; dl = (float)(d - (double)dh);
-        bf = bh; df = dh;
-        const double bd = b * d;
-        bdh = (float)bd; bdl = (float)(bd - (double)bdh);
-    }
+    __device__ __forceinline__ NLConst(const NLSplit &s)
+        : bh(s.bh), bl(s.bl), dh(s.dh), dl(s.dl), bf(s.bh), df(s.dh), bdh(s.bdh), bdl(s.bdl) {}
+    __device__ __forceinline__ NLConst(double b, double d) : NLConst(nl_split(b, d)) {}
 };
+// the NL constants of a pass kernel: FP32 from the host-made split, FP64 as is
+template <typename T> __device__ __forceinline__ NLConst<T> nl_const(const NLSplit &s, double b, double d);
+template <> __device__ __forceinline__ NLConst<float> nl_const<float>(const NLSplit &s, double, double)
+{
+    return NLConst<float>(s);
+}
+template <> __device__ __forceinline__ NLConst<double> nl_const<double>(const NLSplit &, double b, double d)
+{
+    return NLConst<double>(b, d);
+}
 
 // Short path of the FP32 real-time factor, taken by every cell whose
 // |theta| <= NL_SHORT_MAX < pi/4 (no reduction needed): theta from one-float

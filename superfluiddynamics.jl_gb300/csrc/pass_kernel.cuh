@@ -85,7 +85,9 @@ template <typename T> struct PassArgs {
     int nl_mode;
     const T *V;              // nullable (zero potential)
     double nl_beta, nl_dt;
-    // deferred renormalisation: multiply the input by *scale (nullable)
+    NLSplit nl_split;        // FP32 kernels: beta, dt, beta*dt as float pairs
+    // deferred renormalisation: multiply the input by the factor in a
+    // ScaleCell (nullable; `scale` points at its FP64 member)
     const double *scale;
     // reductions: per-CTA FP64 partials, finished by the last CTA to arrive
     int red;                 // RED_POINT | RED_KIN | RED_MASS
@@ -94,12 +96,32 @@ template <typename T> struct PassArgs {
     double *fin_out;         // RQ_COUNT sums of this pass
     int fin_mode;            // FIN_*
     const double *fin_target;  // M0 of the mass lock
-    double *fin_scale;       // factor for the next pass
+    double *fin_scale;       // factor for the next pass (a ScaleCell)
     int *fin_status;         // set to 1 on a non-finite or non-positive mass
     double dV;
-    double kmult;            // xi_k = kk * kmult, kk the signed wavenumber index
+    T kmult;                 // xi_k = kk * kmult, kk the signed wavenumber index
     const double *coord;     // coordinate of each row (rotation energy), nullable
 };
+
+// A renormalisation factor as written by the last CTA of a pass: FP64 for the
+// FP64 kernels and a float copy for the FP32 ones (which then need no FP64
+// conversion per thread).  Device buffers holding one are 16 bytes.
+struct ScaleCell {
+    double d;
+    float f;
+};
+template <typename T> __device__ __forceinline__ T load_scale(const double *p);
+template <> __device__ __forceinline__ float load_scale<float>(const double *p)
+{
+    return reinterpret_cast<const ScaleCell *>(p)->f;
+}
+template <> __device__ __forceinline__ double load_scale<double>(const double *p) { return *p; }
+__device__ __forceinline__ void store_scale(double *p, double v)
+{
+    ScaleCell *c = reinterpret_cast<ScaleCell *>(p);
+    c->d = v;
+    c->f = (float)v;
+}
 
 // a double-word constant in shared memory: hi and lo adjacent, so one
 // 16-byte load (two for FP64) fetches both
@@ -217,11 +239,11 @@ __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned 
             const double m = a.fin_out[RQ_MASS];
             if (!(m > 0.0) || !isfinite(m)) {
                 *a.fin_status = 1;
-                *a.fin_scale = 1.0;
+                store_scale(a.fin_scale, 1.0);
             } else if (a.fin_mode == FIN_MASSLOCK) {
-                *a.fin_scale = sqrt(*a.fin_target / m);
+                store_scale(a.fin_scale, sqrt(*a.fin_target / m));
             } else {
-                *a.fin_scale = 1.0 / (sqrt(m) * sqrt(a.dV));
+                store_scale(a.fin_scale, 1.0 / (sqrt(m) * sqrt(a.dV)));
             }
         }
         *a.counter = 0u;
@@ -261,8 +283,8 @@ pass_kernel(const PassArgs<T> a)
     };
 
     const bool scaled = a.scale != nullptr;
-    const T scale = scaled ? (T)(*a.scale) : (T)1;
-    const T kmult = (T)a.kmult;
+    const T scale = scaled ? load_scale<T>(a.scale) : (T)1;
+    const T kmult = a.kmult;
 
     // accumulators (precision of the field; the CTA totals are kept in FP64)
     T acc_mass = 0, acc_pot = 0, acc_int = 0, acc_kin = 0, acc_rot = 0;
@@ -443,7 +465,7 @@ pass_kernel(const PassArgs<T> a)
     if constexpr (MODE == MODE_FUSED || MODE == MODE_INV) {
         if constexpr (MODE == MODE_FUSED) {
             if (a.nl_mode != NL_NONE) {
-                const NLConst<T> nlc(a.nl_beta, a.nl_dt);
+                const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);
                 const bool imag = a.nl_mode == NL_IMAG;
                 bool done = false;
                 if constexpr (sizeof(T) == 4) {

@@ -111,10 +111,10 @@ pass_pipe_kernel(const PassArgs<T> a, int ntiles)
     };
 
     const bool scaled = a.scale != nullptr;
-    const T scale = scaled ? (T)(*a.scale) : (T)1;
-    const T kmult = (T)a.kmult;
+    const T scale = scaled ? load_scale<T>(a.scale) : (T)1;
+    const T kmult = a.kmult;
     T acc_mass = 0, acc_pot = 0, acc_int = 0, acc_kin = 0, acc_rot = 0;
-    const NLConst<T> nlc(a.nl_beta, a.nl_dt);
+    const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);
     const bool imag = a.nl_mode == NL_IMAG;
     bool timed_out = false;
     int wait_b = 0, pref_b = -1;       // barriers with loads possibly in flight at a timeout
