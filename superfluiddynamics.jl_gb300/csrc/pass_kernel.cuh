@@ -129,16 +129,26 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
     V hi, lo;
 };
 
-// resident CTAs per SM that the FP32 kernels are compiled for.  3 (at most 80
-// registers) measured best at 256^3: 4 (64 registers) spills and runs 15-25%
-// slower, no bound lets the fused kernels grow past 85 registers (2 CTAs per
-// SM) and run 1.7x slower.
-#ifndef GPSS_PASS_MIN_BLOCKS_F32
-#define GPSS_PASS_MIN_BLOCKS_F32 3
+// Threads per CTA and resident CTAs per SM that the kernels are compiled for.
+// FP32: 768 threads per SM (at most 80 registers) measured best at 256^3;
+// 1024 (64 registers) spills and runs 15-25% slower, no bound lets the fused
+// kernels grow past 85 registers and run 1.7x slower.  x lines run in CTAs
+// of 128 threads (8% faster than 256: finer barriers), y/z columns in CTAs of
+// 256 (their global accesses are W = 256/16 = 16 adjacent cells, 128 B; with
+// 128 threads they would be 64 B and run 5% slower).
+#ifndef GPSS_PASS_THREADS_XL_F32
+#define GPSS_PASS_THREADS_XL_F32 128
 #endif
-template <typename T> struct PassGeom {
-    static constexpr int THREADS = 256;
-    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? GPSS_PASS_MIN_BLOCKS_F32 : 1;
+#ifndef GPSS_PASS_THREADS_COL_F32
+#define GPSS_PASS_THREADS_COL_F32 256
+#endif
+#ifndef GPSS_PASS_SM_THREADS_F32
+#define GPSS_PASS_SM_THREADS_F32 768
+#endif
+template <typename T, bool XL> struct PassGeom {
+    static constexpr int THREADS =
+        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : GPSS_PASS_THREADS_COL_F32) : 256;
+    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? GPSS_PASS_SM_THREADS_F32 / THREADS : 1;
 };
 
 template <int N> struct Split {
@@ -150,7 +160,7 @@ template <typename T, int N, bool XL> struct PassShape {
     static constexpr int N1 = Split<N>::N1;
     static constexpr int N2 = Split<N>::N2;
     static constexpr int P = N2;                       // threads per line
-    static constexpr int THREADS = PassGeom<T>::THREADS;
+    static constexpr int THREADS = PassGeom<T, XL>::THREADS;
     static constexpr int W = THREADS / P;              // lines per CTA
     static constexpr int LS = N + N1 + N2;             // XL padded line stride (slots)
     static constexpr int DATA = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
@@ -251,7 +261,7 @@ __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned 
 }
 
 template <typename T, int N, bool XL, int MODE>
-__global__ void __launch_bounds__(PassGeom<T>::THREADS, PassGeom<T>::MIN_BLOCKS)
+__global__ void __launch_bounds__(PassGeom<T, XL>::THREADS, PassGeom<T, XL>::MIN_BLOCKS)
 pass_kernel(const PassArgs<T> a)
 {
     using V = vec2<T>;
