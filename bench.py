@@ -20,6 +20,11 @@ JSON line keys beyond the base contract:
                  sample of the same workload.
   fp64_plain     the FP64 plain kernels (reference stage order) on the same
                  workload, the comparison the headline metric names.
+  batched        cfg3: 512 mixed-size 2D runs in one persistent launch.
+  accuracy       rel-L2 of the FP32 fused field vs the FP64 plain field.
+  imag_time      cfg2: 128^3 imaginary-time steps, FP32 and FP64.
+  adjoint        cfg4: one 2000-step gradient through gpss_adjoint.
+  cufft_comparison  the same directional pass through cuFFT (torch.fft).
 
 --impl reference times the CPU restatement of the reference path (the
 reference itself is Julia + FFTW, which does not exist on this machine).
@@ -60,6 +65,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the accuracy, cfg2, cfg4 and cuFFT measurements")
     return ap.parse_args()
 
 
@@ -248,6 +255,115 @@ def measure_batch(sfd, W, calls=3):
             "max_rel_mass_drift": float(np.max(np.abs(m - m0) / m0))}
 
 
+def _model(sfd, c, precision, form="fused", V=None, steps=1):
+    grid = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(grid)
+    f.phi = c["psi"]
+    pot = sfd.PotentialZero(f) if V is None else sfd.PotentialArray(f, V)
+    p = sfd.GrossPitaevskiiParameters(pot, coeffD=c["coeffD"], beta=c["beta"])
+    return f, sfd.NumModelSplit2(f, p, c["dt"], steps, steps, precision=precision, form=form)
+
+
+def measure_accuracy(sfd, c, marks=(50, 100, 150, 200)):
+    """rel-L2 of the FP32 fused field against the FP64 plain field (the FP64
+    kernels match the oracle to 1e-13 in the tests) after each mark."""
+    f32, m32 = _model(sfd, c, "fp32")
+    f64, m64 = _model(sfd, c, "fp64", "plain")
+    out, done = {}, 0
+    for k in marks:
+        m32.step(k - done)
+        m64.step(k - done)
+        done = k
+        a, b = f32.phi, f64.phi
+        out[str(k)] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    m32.close(download=False)
+    m64.close(download=False)
+    return {"rel_l2_fp32_fused_vs_fp64_plain": out, "bar": 1e-5}
+
+
+def _event_ms(L, h, fn):
+    ms = ctypes.c_float()
+    L.gpss_event_record(h, 0)
+    fn()
+    L.gpss_event_record(h, 1)
+    L.gpss_event_elapsed(h, 0, 1, ctypes.byref(ms))
+    return ms.value
+
+
+def measure_imag(sfd, W, L, steps=200):
+    """cfg2 (128^3 anisotropic trap, imaginary time, per-step FP64 renormalisation):
+    fixed-step throughput of the fused FP32 and FP64 kernels."""
+    c = W.cfg2(128)
+    cells = float(math.prod(c["shape"]))
+    out = {"workload": "cfg2: 3D imaginary-time GP, 128^3 on [-10,10]^3, V=(x^2+y^2+4z^2)/2, g=2000, "
+                       f"dt=1e-3, {steps} steps per timing"}
+    for prec in ("fp32", "fp64"):
+        f, m = _model(sfd, c, prec, V=c["V"])
+        h = m.handle
+        for _ in range(3):
+            L.gpss_step(h, 20, 2, 1, c["dt"], None)
+        ms = _event_ms(L, h, lambda: L.gpss_step(h, steps, 2, 1, c["dt"], None))
+        out[prec] = {"value": cells * steps / (ms / 1e3) / 1e6, "unit": "Mcell-steps/s",
+                     "ms_per_timestep": ms / steps}
+        m.close(download=False)
+    return out
+
+
+def measure_adjoint(sfd, W):
+    """cfg4 (256^2, 2000 steps, checkpoints every 50): one gradient (forward with
+    checkpoints, recompute, backward) through gpss_adjoint, host-timed."""
+    c = W.cfg4(256)
+    out = {"workload": "cfg4: 2D adjoint, 256^2 on [-8,8]^2, trap + learnable V, g=500, dt=1e-3, "
+                       "2000 steps, K=50, loss 1-|<psi_t|psi(T)>|^2"}
+    for prec in ("fp32", "fp64"):
+        f, m = _model(sfd, c, prec, V=c["V"])
+        m.adjoint(c["target"], 100, 50)  # warm-up
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            loss, dv, g0 = m.adjoint(c["target"], c["nsteps"], c["K"])
+            t.append(time.perf_counter() - t0)
+        m.close(download=False)
+        out[prec] = {"s_per_gradient": min(t), "loss": loss,
+                     "forward_plus_backward_cell_steps_per_s": 256 * 256 * c["nsteps"] / min(t)}
+    return out
+
+
+def measure_cufft(c, n, reps=20):
+    """The same directional pass (FFT -> phase multiply -> inverse FFT) through
+    cuFFT (torch.fft, complex64) on the 256^3 field, per axis, for comparison."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+    except ImportError:
+        return None
+    x = torch.from_numpy(np.ascontiguousarray(c["psi"].reshape(-1, order="F")).astype(np.complex64))
+    x = x.cuda().reshape(n, n, n)  # [z][y][x]
+    k = torch.fft.fftfreq(n, d=1.0 / n, device="cuda")
+    ph = torch.exp(1j * (c["coeffD"] * (k * k) * c["dt"]).to(torch.float32)).to(torch.complex64)
+    out = {"note": "torch.fft (cuFFT) complex64 at 256^3, per axis: fft -> multiply by exp(i coeffD k^2 dt) "
+                   "-> ifft, CUDA events, mean of 20"}
+    for dim, name in ((2, "x"), (1, "y"), (0, "z")):
+        shape = [1, 1, 1]
+        shape[dim] = n
+        p = ph.reshape(shape)
+        f = lambda: torch.fft.ifft(torch.fft.fft(x, dim=dim) * p, dim=dim)
+        for _ in range(3):
+            f()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            f()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name + "_pass_ms"] = e0.elapsed_time(e1) / reps
+    del x
+    torch.cuda.empty_cache()
+    return out
+
+
 # ----------------------------------------------------------------- GPU arm --
 def run_gpss(args, rank, world, local):
     import importlib
@@ -361,6 +477,17 @@ def run_gpss(args, rank, world, local):
     if not args.no_batch:
         batch = measure_batch(sfd, W)
 
+    # ---- accuracy, imaginary time (cfg2), adjoint (cfg4), cuFFT comparison
+    extra = {}
+    if not args.no_extra and rank == 0 and args.n == 256:
+        extra["accuracy"] = measure_accuracy(sfd, c)
+        extra["imag_time"] = measure_imag(sfd, W, L)
+        extra["adjoint"] = measure_adjoint(sfd, W)
+        cu = measure_cufft(c, args.n)
+        if cu:
+            cu["gpss_pass_ms"] = per_axis
+            extra["cufft_comparison"] = cu
+
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -401,6 +528,7 @@ def run_gpss(args, rank, world, local):
         "fp64_plain": fp64,
         "batched": batch,
     }
+    line.update(extra)
     if clk:
         line["clocks"] = clk
     print(json.dumps(line), flush=True)
