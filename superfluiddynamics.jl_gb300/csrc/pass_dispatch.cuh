@@ -13,11 +13,11 @@ namespace gpss {
 #define GPSS_PASS_WAVES 1
 #endif
 
-template <typename T, int N, bool XL, int MODE>
+template <typename T, int N, bool XL, int MODE, int FEAT = FEAT_ALL>
 static cudaError_t launch_pass_inst(const PassArgs<T> &a, int tiles, cudaStream_t s)
 {
     using S = PassShape<T, N, XL>;
-    auto k = pass_kernel<T, N, XL, MODE>;
+    auto k = pass_kernel<T, N, XL, MODE, FEAT>;
     static int wave[64] = {0};
     int dev = 0;
     cudaGetDevice(&dev);
@@ -49,7 +49,14 @@ template <typename T, int N, bool XL>
 static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, cudaStream_t s)
 {
     switch (mode) {
-    case MODE_FUSED: return launch_pass_inst<T, N, XL, MODE_FUSED>(a, blocks, s);
+    case MODE_FUSED: {
+        // the leanest instantiation that does everything the arguments ask for
+        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0;
+        const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
+        if (diag) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
+        if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NL>(a, blocks, s);
+        return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NONE>(a, blocks, s);
+    }
     case MODE_FWD: return launch_pass_inst<T, N, XL, MODE_FWD>(a, blocks, s);
     case MODE_INV: return launch_pass_inst<T, N, XL, MODE_INV>(a, blocks, s);
     case MODE_DIAG: return launch_pass_inst<T, N, XL, MODE_DIAG>(a, blocks, s);

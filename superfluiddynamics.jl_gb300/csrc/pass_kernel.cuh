@@ -65,6 +65,12 @@ enum { RED_POINT = 1, RED_KIN = 2, RED_MASS = 4 };
 // lock (sqrt(M0/M)) written to *fin_scale for the next pass
 enum { FIN_NONE = 0, FIN_UNITMASS = 1, FIN_MASSLOCK = 2 };
 enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
+// Optional work a FUSED pass instantiation can do (chosen per launch from the
+// arguments; a leaner instantiation keeps fewer values live, which kept the
+// hot passes free of register spills under the 80-register bound):
+//   FEAT_NL    nonlinear epilogue and the mass sum
+//   FEAT_DIAG  energy sums (RED_POINT, RED_KIN), rotation (per-row phases)
+enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3 };
 
 template <typename T> struct PassArgs {
     const vec2<T> *in;
@@ -260,10 +266,13 @@ __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned 
     }
 }
 
-template <typename T, int N, bool XL, int MODE>
+template <typename T, int N, bool XL, int MODE, int FEAT = FEAT_ALL>
 __global__ void __launch_bounds__(PassGeom<T, XL>::THREADS, PassGeom<T, XL>::MIN_BLOCKS)
 pass_kernel(const PassArgs<T> a)
 {
+    constexpr bool kNL = (FEAT & FEAT_NL) != 0, kDiag = (FEAT & FEAT_DIAG) != 0;
+    const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag ? RED_MASS : 0));
+    const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
     using S = PassShape<T, N, XL>;
     constexpr int N1 = S::N1, N2 = S::N2, P = S::P, W = S::W, LS = S::LS;
@@ -280,7 +289,7 @@ pass_kernel(const PassArgs<T> a)
     for (int i = tid; i < N; i += THREADS) {
         stw[i] = DWord<V>{a.tw[i], a.tw[N + i]};
         stwB[i] = DWord<V>{a.tw[2 * N + i], a.tw[3 * N + i]};
-        if (MODE == MODE_FUSED && a.prow == 0) sph[i] = DWord<V>{a.phase[i], a.phase[N + i]};
+        if (MODE == MODE_FUSED && prow == 0) sph[i] = DWord<V>{a.phase[i], a.phase[N + i]};
     }
 
     const int w = XL ? tid / P : tid % W;
@@ -323,7 +332,7 @@ pass_kernel(const PassArgs<T> a)
             }
         }
         if constexpr (MODE == MODE_DIAG) {
-            if (a.red & RED_POINT) {
+            if (red & RED_POINT) {
 #pragma unroll
                 for (int j = 0; j < N1; j++) {
                     T rho = v[j].x * v[j].x + v[j].y * v[j].y;
@@ -340,7 +349,7 @@ pass_kernel(const PassArgs<T> a)
     if constexpr (N2 == 1) {
         // the whole line lives in this thread: v[k] = X[k]
         if constexpr (MODE == MODE_FUSED) {
-            if (a.red & RED_KIN) {
+            if (red & RED_KIN) {
                 T s2 = 0, s1 = 0;
 #pragma unroll
                 for (int k = 0; k < N1; k++) {
@@ -355,14 +364,14 @@ pass_kernel(const PassArgs<T> a)
             }
 #pragma unroll
             for (int k = 0; k < N1; k++) {
-                const DWord<V> p = a.prow ? DWord<V>{a.phase[row * a.prow + k], a.phase[row * a.prow + N + k]}
+                const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
                                           : sph[k];
                 v[k] = cmul2(v[k], p.hi, p.lo);
                 if (scaled) v[k] = cscale(v[k], scale);
             }
             dft<N1, +1>(v);
         } else if constexpr (MODE == MODE_DIAG) {
-            if (a.red & RED_KIN) {
+            if (red & RED_KIN) {
                 T s2 = 0, s1 = 0;
 #pragma unroll
                 for (int k = 0; k < N1; k++) {
@@ -421,7 +430,7 @@ pass_kernel(const PassArgs<T> a)
                 continue;
             }
             if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
-                if (a.red & RED_KIN) {
+                if (red & RED_KIN) {
                     T s2 = 0, s1 = 0;
 #pragma unroll
                     for (int k2 = 0; k2 < N2; k2++) {
@@ -441,7 +450,7 @@ pass_kernel(const PassArgs<T> a)
 #pragma unroll
                 for (int k2 = 0; k2 < N2; k2++) {
                     const int k = k1 + N1 * k2;
-                    const DWord<V> p = a.prow ? DWord<V>{a.phase[row * a.prow + k], a.phase[row * a.prow + N + k]}
+                    const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
                                               : sph[k];
                     u[k2] = cmul2(u[k2], p.hi, p.lo);
                     if (scaled) u[k2] = cscale(u[k2], scale);
@@ -474,7 +483,7 @@ pass_kernel(const PassArgs<T> a)
     // ---- epilogue: positions r + N2 j
     if constexpr (MODE == MODE_FUSED || MODE == MODE_INV) {
         if constexpr (MODE == MODE_FUSED) {
-            if (a.nl_mode != NL_NONE) {
+            if (kNL && a.nl_mode != NL_NONE) {
                 const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);
                 const bool imag = a.nl_mode == NL_IMAG;
                 bool done = false;
@@ -514,7 +523,7 @@ pass_kernel(const PassArgs<T> a)
                     }
                 }
             }
-            if (a.red & RED_POINT) {
+            if (red & RED_POINT) {
 #pragma unroll
                 for (int j = 0; j < N1; j++) {
                     const T rho = v[j].x * v[j].x + v[j].y * v[j].y;
@@ -522,7 +531,7 @@ pass_kernel(const PassArgs<T> a)
                     acc_int += rho * rho;
                     if (a.V) acc_pot += a.V[base + (uint32_t)(r + N2 * j) * st] * rho;
                 }
-            } else if (a.red & RED_MASS) {
+            } else if (red & RED_MASS) {
 #pragma unroll
                 for (int j = 0; j < N1; j++) acc_mass += v[j].x * v[j].x + v[j].y * v[j].y;
             }
@@ -541,11 +550,11 @@ pass_kernel(const PassArgs<T> a)
     }  // tiles
 
     if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
-        if (a.red) {
+        if (red) {
             unsigned qmask = 0;
-            if (a.red & (RED_POINT | RED_MASS)) qmask |= 1u << RQ_MASS;
-            if (a.red & RED_POINT) qmask |= (1u << RQ_POT) | (1u << RQ_INT);
-            if (a.red & RED_KIN) qmask |= (1u << RQ_KIN) | (1u << RQ_ROT);
+            if (red & (RED_POINT | RED_MASS)) qmask |= 1u << RQ_MASS;
+            if (red & RED_POINT) qmask |= (1u << RQ_POT) | (1u << RQ_INT);
+            if (red & RED_KIN) qmask |= (1u << RQ_KIN) | (1u << RQ_ROT);
             const T vals[RQ_COUNT] = {acc_mass, acc_pot, acc_int, acc_kin, acc_rot};
             block_sums_store<T, THREADS>(vals, qmask, a.partials);
             finish_reduction<T, THREADS>(a, qmask);
