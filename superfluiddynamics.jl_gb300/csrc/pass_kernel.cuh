@@ -151,10 +151,21 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #ifndef GPSS_PASS_SM_THREADS_F32
 #define GPSS_PASS_SM_THREADS_F32 768
 #endif
+// the lean FUSED y/z instantiation (FEAT_NONE: kinetic pass only) fits 64
+// registers without spills, so it is compiled for 1024 threads per SM (y pass
+// 69.5 -> 67.2 us at 256^3; the x one spills at 64 and runs 6% slower)
+#ifndef GPSS_PASS_SM_THREADS_LEAN_F32
+#define GPSS_PASS_SM_THREADS_LEAN_F32 1024
+#endif
 template <typename T, bool XL> struct PassGeom {
     static constexpr int THREADS =
         sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : GPSS_PASS_THREADS_COL_F32) : 256;
-    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? GPSS_PASS_SM_THREADS_F32 / THREADS : 1;
+};
+template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
+    static constexpr int SM_THREADS =
+        (MODE == MODE_FUSED && FEAT == FEAT_NONE && !XL) ? GPSS_PASS_SM_THREADS_LEAN_F32
+                                                         : GPSS_PASS_SM_THREADS_F32;
+    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? SM_THREADS / PassGeom<T, XL>::THREADS : 1;
 };
 
 template <int N> struct Split {
@@ -170,7 +181,10 @@ template <typename T, int N, bool XL> struct PassShape {
     static constexpr int W = THREADS / P;              // lines per CTA
     static constexpr int LS = N + N1 + N2;             // XL padded line stride (slots)
     static constexpr int DATA = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
-    static constexpr int SMEM_SLOTS = DATA + 6 * N;    // + twiddles (A, B) + phase, hi and lo
+    // w_n^{r k1} at k1*N2 + r (stage A) and at r*N1 + k1 (stage B) are the same
+    // table when N1 == N2: then only one is held
+    static constexpr bool TWB = N1 != N2;
+    static constexpr int SMEM_SLOTS = DATA + (TWB ? 6 : 4) * N;  // + twiddles + phase, hi and lo
     static constexpr size_t SMEM_BYTES = sizeof(vec2<T>) * SMEM_SLOTS;
 };
 
@@ -267,7 +281,7 @@ __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned 
 }
 
 template <typename T, int N, bool XL, int MODE, int FEAT = FEAT_ALL>
-__global__ void __launch_bounds__(PassGeom<T, XL>::THREADS, PassGeom<T, XL>::MIN_BLOCKS)
+__global__ void __launch_bounds__(PassGeom<T, XL>::THREADS, PassOcc<T, XL, MODE, FEAT>::MIN_BLOCKS)
 pass_kernel(const PassArgs<T> a)
 {
     constexpr bool kNL = (FEAT & FEAT_NL) != 0, kDiag = (FEAT & FEAT_DIAG) != 0;
@@ -281,14 +295,14 @@ pass_kernel(const PassArgs<T> a)
     extern __shared__ __align__(32) unsigned char smem_raw[];
     V *sdata = reinterpret_cast<V *>(smem_raw);
     DWord<V> *stw = reinterpret_cast<DWord<V> *>(sdata + S::DATA);  // stage A [N], stage B [N]
-    DWord<V> *stwB = stw + N;
-    DWord<V> *sph = stw + 2 * N;                                      // phase [N]
+    DWord<V> *stwB = S::TWB ? stw + N : stw;
+    DWord<V> *sph = stw + (S::TWB ? 2 : 1) * N;                      // phase [N]
 
     const int tid = threadIdx.x;
     // tables into shared memory, hi/lo halves packed per entry
     for (int i = tid; i < N; i += THREADS) {
         stw[i] = DWord<V>{a.tw[i], a.tw[N + i]};
-        stwB[i] = DWord<V>{a.tw[2 * N + i], a.tw[3 * N + i]};
+        if (S::TWB) stwB[i] = DWord<V>{a.tw[2 * N + i], a.tw[3 * N + i]};
         if (MODE == MODE_FUSED && prow == 0) sph[i] = DWord<V>{a.phase[i], a.phase[N + i]};
     }
 
