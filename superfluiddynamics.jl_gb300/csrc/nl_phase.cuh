@@ -112,19 +112,31 @@ __device__ __forceinline__ float nl_theta_short(float2 v, float Vv, const NLCons
     if (Vv != 0.0f) th = fmaf(Vv, c.dh, fmaf(Vv, c.dl, th));
     return th;
 }
+// For |theta| <= NL_TINY_MAX shorter series suffice: sin to degree 5 and cos
+// to degree 6 truncate below 8e-10 relative there.
+#define NL_TINY_MAX 0.125f
+__device__ __forceinline__ float2 nl_factor_tiny(float th)
+{
+    const float z = th * th;
+    const float sf = fmaf(th * z, fmaf(z, 1.0f / 120.0f, -1.0f / 6.0f), th);
+    const float cf = fmaf(z, fmaf(z, fmaf(z, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
+    return make_float2(cf, -sf);
+}
+// exp(-i theta) for |theta| <= NL_SHORT_MAX, by the series of its size class
 __device__ __forceinline__ float2 nl_factor_short(float th)
 {
+    if (fabsf(th) <= NL_TINY_MAX) return nl_factor_tiny(th);
     float sf, cf;
     sincos_reduced(th, &sf, &cf);
     return make_float2(cf, -sf);
 }
-// True when every cell with |psi|^2 <= rmax and |V| <= vmax takes the short
-// path (a bound on |nl_theta_short| with a margin far above its rounding), so
-// a warp that agrees on it may call nl_factor_short directly and still
-// produce exactly what nl_factor gives cell by cell.
-__device__ __forceinline__ bool nl_short_bound(float rmax, float vmax, const NLConst<float> &c)
+// A bound on |nl_theta_short| over every cell with |psi|^2 <= rmax and
+// |V| <= vmax, with a margin far above its rounding: a warp whose bound is
+// <= NL_TINY_MAX (NL_SHORT_MAX) may call nl_factor_tiny (nl_factor_short)
+// directly and still produce exactly what nl_factor gives cell by cell.
+__device__ __forceinline__ float nl_theta_bound(float rmax, float vmax, const NLConst<float> &c)
 {
-    return (fabsf(c.bdh) * rmax + fabsf(c.dh) * vmax) * 1.001f <= NL_SHORT_MAX;
+    return (fabsf(c.bdh) * rmax + fabsf(c.dh) * vmax) * 1.001f;
 }
 
 // The factor f = exp(-i theta) (real time) or exp(-theta) (imaginary time,
@@ -202,6 +214,15 @@ __device__ __forceinline__ float2 nl_apply(float2 v, float Vv, const NLConst<flo
     const float2 f = nl_factor(v, Vv, c, imag);
     if (imag) return make_float2(f.x * v.x, f.x * v.y);
     return nl_rotate(f, v);
+}
+
+// The FP32 real-time step of one cell as an out-of-line call, for the pass
+// kernels' fallback when a warp's cells do not all take the short path: the
+// double-float evaluation's temporaries then do not count against the
+// registers of the kernel's common path.
+static __device__ __noinline__ float2 nl_apply_real_cell(float2 v, float Vv, NLConst<float> c)
+{
+    return nl_apply(v, Vv, c, false);
 }
 
 }  // namespace gpss

@@ -504,7 +504,7 @@ pass_kernel(const PassArgs<T> a)
                 if constexpr (sizeof(T) == 4) {
                     if (!imag) {
                         // one vote per warp: if every cell of the warp takes the
-                        // short path, skip the per-cell choice
+                        // tiny (short) path, skip the per-cell choice
                         T rmax = 0, vmax = 0;
 #pragma unroll
                         for (int j = 0; j < N1; j++) rmax = fmaxf(rmax, fmaf(v[j].x, v[j].x, v[j].y * v[j].y));
@@ -513,17 +513,25 @@ pass_kernel(const PassArgs<T> a)
                             for (int j = 0; j < N1; j++)
                                 vmax = fmaxf(vmax, fabsf(a.V[base + (uint32_t)(r + N2 * j) * st]));
                         }
-                        if (__all_sync(0xffffffffu, nl_short_bound(rmax, vmax, nlc))) {
+                        const T tb = nl_theta_bound(rmax, vmax, nlc);
+                        if (__all_sync(0xffffffffu, tb <= NL_TINY_MAX)) {
                             if (a.V) {
 #pragma unroll
                                 for (int j = 0; j < N1; j++) {
                                     const T vv = a.V[base + (uint32_t)(r + N2 * j) * st];
-                                    v[j] = nl_rotate(nl_factor_short(nl_theta_short(v[j], vv, nlc)), v[j]);
+                                    v[j] = nl_rotate(nl_factor_tiny(nl_theta_short(v[j], vv, nlc)), v[j]);
                                 }
                             } else {
 #pragma unroll
                                 for (int j = 0; j < N1; j++)
-                                    v[j] = nl_rotate(nl_factor_short(nl_theta_short(v[j], (T)0, nlc)), v[j]);
+                                    v[j] = nl_rotate(nl_factor_tiny(nl_theta_short(v[j], (T)0, nlc)), v[j]);
+                            }
+                            done = true;
+                        } else if (__all_sync(0xffffffffu, tb <= NL_SHORT_MAX)) {
+#pragma unroll
+                            for (int j = 0; j < N1; j++) {
+                                const T vv = a.V ? a.V[base + (uint32_t)(r + N2 * j) * st] : (T)0;
+                                v[j] = nl_rotate(nl_factor_short(nl_theta_short(v[j], vv, nlc)), v[j]);
                             }
                             done = true;
                         }
@@ -533,7 +541,11 @@ pass_kernel(const PassArgs<T> a)
 #pragma unroll
                     for (int j = 0; j < N1; j++) {
                         const T vv = a.V ? a.V[base + (uint32_t)(r + N2 * j) * st] : (T)0;
-                        v[j] = nl_apply(v[j], vv, nlc, imag);
+                        if constexpr (sizeof(T) == 4) {
+                            v[j] = imag ? nl_apply(v[j], vv, nlc, true) : nl_apply_real_cell(v[j], vv, nlc);
+                        } else {
+                            v[j] = nl_apply(v[j], vv, nlc, imag);
+                        }
                     }
                 }
             }
