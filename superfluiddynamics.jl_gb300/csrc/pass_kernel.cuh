@@ -153,9 +153,13 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #endif
 // the lean FUSED y/z instantiation (FEAT_NONE: kinetic pass only) fits 64
 // registers without spills, so it is compiled for 1024 threads per SM (y pass
-// 69.5 -> 67.2 us at 256^3; the x one spills at 64 and runs 6% slower)
+// 69.5 -> 67.2 us at 256^3); the x one spills at 64 (6% slower) but fits 72
+// (896 threads per SM).  The NL instantiation spills at 64 (1% slower).
 #ifndef GPSS_PASS_SM_THREADS_LEAN_F32
 #define GPSS_PASS_SM_THREADS_LEAN_F32 1024
+#endif
+#ifndef GPSS_PASS_SM_THREADS_LEAN_XL_F32
+#define GPSS_PASS_SM_THREADS_LEAN_XL_F32 896  // 7 CTAs of 128, 72 registers: x 63.8 -> 61.9 us
 #endif
 template <typename T, bool XL> struct PassGeom {
     static constexpr int THREADS =
@@ -163,8 +167,9 @@ template <typename T, bool XL> struct PassGeom {
 };
 template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
     static constexpr int SM_THREADS =
-        (MODE == MODE_FUSED && FEAT == FEAT_NONE && !XL) ? GPSS_PASS_SM_THREADS_LEAN_F32
-                                                         : GPSS_PASS_SM_THREADS_F32;
+        (MODE == MODE_FUSED && FEAT == FEAT_NONE)
+            ? (XL ? GPSS_PASS_SM_THREADS_LEAN_XL_F32 : GPSS_PASS_SM_THREADS_LEAN_F32)
+            : GPSS_PASS_SM_THREADS_F32;
     static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? SM_THREADS / PassGeom<T, XL>::THREADS : 1;
 };
 
