@@ -106,6 +106,20 @@ int gpss_download(gpss_ctx *ctx, double *psi);
 int gpss_step(gpss_ctx *ctx, int nsteps, int scheme, int imag, double dt, gpss_diag *diag);
 
 /*
+ * nsteps explicit Runge-Kutta steps of size dt of the time-dependent GP
+ * equation, dpsi/dt = i [lapRot(psi) - (V + beta|psi|^2) psi]: replaces
+ * timeStep!(::NumModelGPRK) (src/NumModels/GrossPitaevskii/explicit-rk.jl:135-166,
+ * right-hand side gp_rhs! :96-107, lapRot GrossPitaevskii.jl:12-45).
+ * stepper: 1 forward Euler ("RK1"), 2 explicit midpoint ("RK2"), 4 classical
+ * RK4 ("RK4").  filter: GPSS_RK_FILTER_* -- where the 2/3 rule (modes with
+ * |xi|^2 >= (4/9) min_d max xi_d^2 zeroed, Plans.jl:529-532) is applied.
+ */
+#define GPSS_RK_FILTER_NONE 0
+#define GPSS_RK_FILTER_PRODUCT 1   /* on the nonlinear term of every stage */
+#define GPSS_RK_FILTER_SOLUTION 2  /* on the state after every step */
+int gpss_rk_step(gpss_ctx *ctx, int nsteps, int stepper, int filter, double dt);
+
+/*
  * Energies of the current field: out = {E_Omega, E_Delta, E_beta, E, mu}.
  * Replaces energy(n) (src/NumModels/GrossPitaevskii/GrossPitaevskii.jl:61-92 2D,
  * 106-136 3D; the 3D method prints no mu, the 2D formula is used for it).

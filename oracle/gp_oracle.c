@@ -18,6 +18,10 @@
  *   norm            src/Discretization/Fields.jl:172-180
  *   energy          src/NumModels/GrossPitaevskii/GrossPitaevskii.jl:61-136 with
  *                   computeDerivatives!(GradientRotField) src/NumModels/derivatives.jl:27-56, 90-126
+ *   explicit RK     src/NumModels/GrossPitaevskii/explicit-rk.jl:96-166 (NumModelGPRK:
+ *                   RK1/RK2/RK4, 2/3-rule filter on the nonlinear term or the state),
+ *                   lapRot GrossPitaevskii.jl:12-45, xi_max Plans.jl:529-532,
+ *                   _dealias_scalar! NavierStokes/NSGP.jl:354-361
  *   imaginary time  extension (no split-step counterpart in the reference): the
  *                   same stages with t -> -i tau and a unit-mass renormalisation
  *                   (normalize!, Fields.jl:196-200) after every step.
@@ -640,6 +644,200 @@ int OR_SYM(or_energy)(int ndim, const int64_t *n, const double *lo, const double
 done:
     for (int a = 0; a < 3; a++) free(d[a]);
     free(rx); free(ry); free(tmp); free(Vr); free(p);
+    grid_free(&g);
+    return rc;
+}
+
+/* ------------------------------------------------ explicit Runge-Kutta -- */
+
+/* Full ND transform, mul_all!/ldiv_all! (Plans.jl:1177-1280): every axis of
+ * every line in turn; the inverse scales once by 1/N at the end, as the
+ * normalised plan_ifft (AbstractFFTs.ScaledPlan) does. */
+static void fft_all(const ogrid *g, ocplx *p, int inverse)
+{
+    for (int a = 0; a < g->ndim; a++) {
+        int64_t len = g->n[a], stride = line_stride(g, a), nlines = g->total / len;
+#pragma omp parallel
+        {
+            ocplx *line = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+            ocplx *tmp = (ocplx *)malloc(sizeof(ocplx) * (size_t)len);
+#pragma omp for schedule(static)
+            for (int64_t l = 0; l < nlines; l++) {
+                int64_t base = line_base(g, a, l);
+                for (int64_t q = 0; q < len; q++) line[q] = p[base + q * stride];
+                fft_line(&g->plan[a], line, tmp, inverse ? +1 : -1);
+                for (int64_t q = 0; q < len; q++) p[base + q * stride] = line[q];
+            }
+            free(line); free(tmp);
+        }
+    }
+    if (inverse) {
+        real s = (real)1 / (real)g->total;
+        int64_t N = g->total;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; i++) { p[i].re *= s; p[i].im *= s; }
+    }
+}
+
+/* 2/3-rule bound (4/9) min_d max|xi_d|^2, Plans.jl:529-532 (Float64) */
+static double xi_max_global(const ogrid *g)
+{
+    double m = 0;
+    for (int a = 0; a < g->ndim; a++) {
+        double ma = 0;
+        for (int64_t k = 0; k < g->n[a]; k++) {
+            double v = g->xi[a][k] * g->xi[a][k];
+            if (v > ma) ma = v;
+        }
+        if (a == 0 || ma < m) m = ma;
+    }
+    return (4.0 / 9.0) * m;
+}
+
+/* _dealias_scalar! (NavierStokes/NSGP.jl:354-361): zero every mode with
+ * xi_x^2 + xi_y^2 [+ xi_z^2] >= xi_max (the sum in Float64, left to right) */
+static void dealias(const ogrid *g, ocplx *p, double xmax)
+{
+    int64_t nx = g->n[0], ny = g->n[1], N = g->total;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        int64_t ix = i % nx, iy = (i / nx) % ny, iz = i / (nx * ny);
+        double k2 = g->xi[0][ix] * g->xi[0][ix];
+        if (g->ndim >= 2) k2 = k2 + g->xi[1][iy] * g->xi[1][iy];
+        if (g->ndim >= 3) k2 = k2 + g->xi[2][iz] * g->xi[2][iz];
+        if (!(k2 < xmax)) { p[i].re = 0; p[i].im = 0; }
+    }
+}
+
+typedef struct {
+    const ogrid *g;
+    const real *V;
+    real beta, cD, Om;
+    int filter;          /* 0 none, 1 product, 2 solution */
+    double xmax;
+    ocplx *dd[3], *rr[2], *nl;   /* scratch */
+} rk_ctx;
+
+/* gp_rhs! (explicit-rk.jl:96-107):
+ *   out = i (lapRot(psi) - N(psi)),  N = (V + beta|psi|^2) psi, 2/3-filtered
+ *   when filter = product (_gp_nl!, :117-124);
+ * lapRot (GrossPitaevskii.jl:12-45) = -cD (ddx + ddy [+ ddz]) + (Om i)(rx + ry). */
+static void gp_rhs(rk_ctx *c, const ocplx *psi, ocplx *out)
+{
+    const ogrid *g = c->g;
+    ocplx *d2[3] = {c->dd[0], g->ndim > 1 ? c->dd[1] : NULL, g->ndim > 2 ? c->dd[2] : NULL};
+    ocplx *rr[3] = {c->rr[0], g->ndim > 1 ? c->rr[1] : NULL, NULL};
+    ocplx *d1[3] = {NULL, NULL, NULL};
+    derivatives(g, psi, d1, d2, rr);
+    int64_t N = g->total;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        real r2 = psi[i].re * psi[i].re + psi[i].im * psi[i].im;
+        real f = (c->V ? c->V[i] : 0) + c->beta * r2;
+        c->nl[i].re = f * psi[i].re;
+        c->nl[i].im = f * psi[i].im;
+    }
+    if (c->filter == 1) {
+        fft_all(g, c->nl, 0);
+        dealias(g, c->nl, c->xmax);
+        fft_all(g, c->nl, 1);
+    }
+    const real mcD = -c->cD;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        ocplx lap = c->dd[0][i];
+        if (g->ndim > 1) { lap.re = lap.re + c->dd[1][i].re; lap.im = lap.im + c->dd[1][i].im; }
+        if (g->ndim > 2) { lap.re = lap.re + c->dd[2][i].re; lap.im = lap.im + c->dd[2][i].im; }
+        ocplx rot = c->rr[0][i];
+        if (g->ndim > 1) { rot.re = rot.re + c->rr[1][i].re; rot.im = rot.im + c->rr[1][i].im; }
+        /* -cD * lap + (0 + Om i) * rot */
+        real lr = mcD * lap.re - c->Om * rot.im;
+        real li = mcD * lap.im + c->Om * rot.re;
+        real dr = lr - c->nl[i].re, di = li - c->nl[i].im;
+        out[i].re = -di;   /* i * (lin - nl) */
+        out[i].im = dr;
+    }
+}
+
+/*
+ * nsteps explicit RK steps, timeStep!(::NumModelGPRK), explicit-rk.jl:135-166:
+ * stepper 1 forward Euler, 2 explicit midpoint, 4 classical RK4; filter 0 none,
+ * 1 the 2/3 rule on the nonlinear term of every stage, 2 on the state after
+ * every step.  The scalar factors are formed as Julia evaluates them
+ * (0.5 * dt first, dt / 6 first; k1 + 2k2 + 2k3 + k4 left to right).
+ */
+int OR_SYM(or_rk_step)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                       double cD, double beta, double Om, const double *V, double *psi,
+                       int nsteps, int stepper, int filter, double dt, int nthreads)
+{
+    if (stepper != 1 && stepper != 2 && stepper != 4) return -1;
+    if (filter < 0 || filter > 2) return -1;
+    ogrid g;
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    int64_t N = g.total;
+    rk_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.g = &g; c.beta = (real)beta; c.cD = (real)cD; c.Om = (real)Om; c.filter = filter;
+    c.xmax = xi_max_global(&g);
+    ocplx *p = load_field(psi, N);
+    real *Vr = load_real(V, N);
+    c.V = Vr;
+    ocplx *k[4] = {NULL, NULL, NULL, NULL}, *st = NULL;
+    int rc = (p && (!V || Vr)) ? 0 : -1;
+    for (int a = 0; a < 3 && rc == 0; a++)
+        if (!(c.dd[a] = (ocplx *)calloc((size_t)N, sizeof(ocplx)))) rc = -1;
+    for (int a = 0; a < 2 && rc == 0; a++)
+        if (!(c.rr[a] = (ocplx *)calloc((size_t)N, sizeof(ocplx)))) rc = -1;
+    if (rc == 0 && !(c.nl = (ocplx *)calloc((size_t)N, sizeof(ocplx)))) rc = -1;
+    for (int a = 0; a < 4 && rc == 0; a++)
+        if (!(k[a] = (ocplx *)calloc((size_t)N, sizeof(ocplx)))) rc = -1;
+    if (rc == 0 && !(st = (ocplx *)calloc((size_t)N, sizeof(ocplx)))) rc = -1;
+#ifdef _OPENMP
+    int saved = omp_get_max_threads();
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    const real Dt = (real)dt, half = (real)(0.5 * dt), sixth = (real)(dt / 6);
+    for (int s = 0; rc == 0 && s < nsteps; s++) {
+        if (stepper == 1) {
+            gp_rhs(&c, p, k[0]);
+            for (int64_t i = 0; i < N; i++) { p[i].re = p[i].re + Dt * k[0][i].re; p[i].im = p[i].im + Dt * k[0][i].im; }
+        } else if (stepper == 2) {
+            gp_rhs(&c, p, k[0]);
+            for (int64_t i = 0; i < N; i++) { st[i].re = p[i].re + half * k[0][i].re; st[i].im = p[i].im + half * k[0][i].im; }
+            gp_rhs(&c, st, k[1]);
+            for (int64_t i = 0; i < N; i++) { p[i].re = p[i].re + Dt * k[1][i].re; p[i].im = p[i].im + Dt * k[1][i].im; }
+        } else {
+            gp_rhs(&c, p, k[0]);
+            for (int64_t i = 0; i < N; i++) { st[i].re = p[i].re + half * k[0][i].re; st[i].im = p[i].im + half * k[0][i].im; }
+            gp_rhs(&c, st, k[1]);
+            for (int64_t i = 0; i < N; i++) { st[i].re = p[i].re + half * k[1][i].re; st[i].im = p[i].im + half * k[1][i].im; }
+            gp_rhs(&c, st, k[2]);
+            for (int64_t i = 0; i < N; i++) { st[i].re = p[i].re + Dt * k[2][i].re; st[i].im = p[i].im + Dt * k[2][i].im; }
+            gp_rhs(&c, st, k[3]);
+            for (int64_t i = 0; i < N; i++) {
+                real sr = k[0][i].re + 2 * k[1][i].re, si = k[0][i].im + 2 * k[1][i].im;
+                sr = sr + 2 * k[2][i].re; si = si + 2 * k[2][i].im;
+                sr = sr + k[3][i].re; si = si + k[3][i].im;
+                p[i].re = p[i].re + sixth * sr;
+                p[i].im = p[i].im + sixth * si;
+            }
+        }
+        if (filter == 2) {
+            fft_all(&g, p, 0);
+            dealias(&g, p, c.xmax);
+            fft_all(&g, p, 1);
+        }
+    }
+#ifdef _OPENMP
+    omp_set_num_threads(saved);
+#endif
+    if (rc == 0) store_field(p, psi, N);
+    for (int a = 0; a < 3; a++) free(c.dd[a]);
+    for (int a = 0; a < 2; a++) free(c.rr[a]);
+    for (int a = 0; a < 4; a++) free(k[a]);
+    free(c.nl); free(st); free(p); free(Vr);
     grid_free(&g);
     return rc;
 }

@@ -33,8 +33,8 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 
 def build(force: bool = False) -> str:
     """Compile gp_oracle.c (FP64 and extended builds) with oracle/Makefile."""
-    if force or not (os.path.exists(_LIB_PATH) and os.path.exists(_EXT_PATH)):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    # make rebuilds only what is out of date
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 
@@ -62,6 +62,10 @@ class _Bound:
         self.or_energy = g("or_energy")
         self.or_energy.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, _f64p, _f64p, _f64p]
+        self.or_rk_step = g("or_rk_step")
+        self.or_rk_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         self.or_max_threads = g("or_max_threads")
         self.or_max_threads.restype = ctypes.c_int
 
@@ -162,6 +166,82 @@ def c_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, s
     if rc != 0:
         raise ValueError("or_step failed")
     return out
+
+
+RK_STEPPERS = {"RK1": 1, "RK2": 2, "RK4": 4}
+RK_FILTERS = {"none": 0, "product": 1, "solution": 2}
+
+
+def c_rk_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, stepper="RK4",
+              filter="product", dt=1e-3, nthreads=0, extended=False):
+    """nsteps of NumModelGPRK.timeStep! (explicit-rk.jl:135-166)."""
+    out = _field(psi).copy(order="F")
+    nd, n, lo, hi = _geom(out.shape, bounds)
+    Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
+    rc = lib(extended).or_rk_step(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
+                                  _p(Vp), _p(out), int(nsteps), RK_STEPPERS[stepper], RK_FILTERS[filter],
+                                  float(dt), int(nthreads))
+    if rc != 0:
+        raise ValueError("or_rk_step failed")
+    return out
+
+
+def np_rk_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, stepper="RK4",
+               filter="product", dt=1e-3):
+    """Same scheme as c_rk_step with numpy.fft (an independent transform): the
+    right-hand side i[(sum_d L_d) psi - N(psi)] with L_d the per-axis spectral
+    multipliers of lapRot (cD xi_x^2 - Om y xi_x, cD xi_y^2 + Om x xi_y, cD xi_z^2)."""
+    p = np.array(psi, dtype=np.complex128, order="F", copy=True)
+    nd = p.ndim
+    shape = p.shape
+    d = spacing(shape, bounds)
+    xs = [grid_coords(n, b[0], b[1]) for n, b in zip(shape, bounds)]
+    xis = [fftfreq(n, dd) for n, dd in zip(shape, d)]
+    Vv = 0.0 if V is None else np.asarray(V, dtype=np.float64)
+
+    def bshape(v, axis):
+        s = [1] * nd
+        s[axis] = v.size
+        return v.reshape(s)
+
+    xmax = (4.0 / 9.0) * min(float(np.max(x * x)) for x in xis)
+    k2 = sum(bshape(x, a) ** 2 for a, x in enumerate(xis))
+    mask = k2 < xmax
+
+    def filt(f):
+        return np.fft.ifftn(mask * np.fft.fftn(f))
+
+    def rhs(q):
+        lin = np.zeros_like(q)
+        for a in range(nd):
+            xi = bshape(xis[a], a)
+            if a == 0 and nd >= 2:
+                m = coeffD * (xi * xi) - omega * bshape(xs[1], 1) * xi
+            elif a == 1:
+                m = coeffD * (xi * xi) + omega * bshape(xs[0], 0) * xi
+            else:
+                m = coeffD * (xi * xi)
+            lin += np.fft.ifft(m * np.fft.fft(q, axis=a), axis=a)
+        nlt = (Vv + beta * (q.real ** 2 + q.imag ** 2)) * q
+        if filter == "product":
+            nlt = filt(nlt)
+        return 1j * (lin - nlt)
+
+    for _ in range(nsteps):
+        if stepper == "RK1":
+            p = p + dt * rhs(p)
+        elif stepper == "RK2":
+            k1 = rhs(p)
+            p = p + dt * rhs(p + 0.5 * dt * k1)
+        else:
+            k1 = rhs(p)
+            k2 = rhs(p + 0.5 * dt * k1)
+            k3 = rhs(p + 0.5 * dt * k2)
+            k4 = rhs(p + dt * k3)
+            p = p + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        if filter == "solution":
+            p = filt(p)
+    return np.asfortranarray(p)
 
 
 def c_derivatives(psi, bounds):

@@ -38,7 +38,7 @@ from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_NOMASSLOCK, GPSS_F
 
 __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "PotentialZero",
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
-           "solve", "BatchSplit2", "GPSSError", "version"]
+           "solve", "BatchSplit2", "GPSSError", "version", "NumModelGPRK"]
 
 _f64p = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -354,6 +354,44 @@ class NumModelSplit1(_SplitModel):
 class NumModelSplit2(_SplitModel):
     """Second-order Strang splitting, L(dt/2) N(dt) L(dt/2) (splitting.jl:84-154)."""
     scheme = 2
+
+
+class NumModelGPRK(_SplitModel):
+    """Explicit Runge-Kutta integrator of the time-dependent GP equation,
+    NumModelGPRK(f, param, dt, niter, freqbckp; stepper="RK4", filter=:product)
+    (explicit-rk.jl:1-167): stepper "RK1" | "RK2" | "RK4", filter "product"
+    (2/3 rule on the nonlinear term of every stage) | "solution" (on the state
+    after every step) | "none".  timeStep returns 0 as the reference does."""
+    scheme = 0
+    _STEPPERS = {"RK1": 1, "RK2": 2, "RK4": 4}
+    _FILTERS = {"none": 0, "product": 1, "solution": 2}
+
+    def __init__(self, f: Field, param: GrossPitaevskiiParameters, dt, niter, freqbckp, *,
+                 stepper="RK4", filter="product", precision="fp64", writers=()):
+        filt = filter.lstrip(":") if isinstance(filter, str) else filter
+        if filt not in self._FILTERS:
+            raise ValueError(f"NumModelGPRK filter {filter} unknown (use :product, :solution or :none).")
+        self.stepper = stepper
+        self.filter = filt
+        super().__init__(f, param, dt, niter, freqbckp, precision=precision, writers=writers)
+
+    def step(self, nsteps=1, imag=False, diag=False):
+        if imag:
+            raise ValueError("NumModelGPRK integrates in real time only")
+        if self.stepper not in self._STEPPERS:
+            raise ValueError(f'NumModelGPRK stepper "{self.stepper}" unknown (use "RK1", "RK2" or "RK4").')
+        self._ck(_lib.lib().gpss_rk_step(self._h, int(nsteps), self._STEPPERS[self.stepper],
+                                         self._FILTERS[self.filter], self.dt))
+        self._device_newer = True
+        if diag:
+            eom, edel, ebeta, e, mu = self.energies()
+            return {"mass": self.mass(), "energy": (eom, edel, ebeta, e, mu), "steps": int(nsteps)}
+        return None
+
+    def __repr__(self):
+        return (f"Gross-Pitaevskii explicit {self.stepper} (2/3 filter: {self.filter})\n"
+                f"  ├───────  time step: {self.dt}\n"
+                f"  └──────────── solve: number of iterations {self.niter}, backup frequency {self.freqbckp}")
 
 
 def timeStep(n: _SplitModel, nsteps: int = 1) -> int:

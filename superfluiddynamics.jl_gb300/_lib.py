@@ -63,6 +63,7 @@ SIGNATURES = {
     "gpss_download": (ctypes.c_int, [_vp, _f64p]),
     "gpss_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                  ctypes.POINTER(Diag)]),
+    "gpss_rk_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
     "gpss_energy": (ctypes.c_int, [_vp, _f64p]),
     "gpss_mass": (ctypes.c_int, [_vp, _f64p]),
     "gpss_norm": (ctypes.c_int, [_vp, _f64p]),

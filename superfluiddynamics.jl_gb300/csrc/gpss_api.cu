@@ -48,6 +48,8 @@ struct gpss_ctx {
     int *status = nullptr;    // [1]
     unsigned int *counter = nullptr;  // arrival counter of the in-kernel reduction finish
     std::vector<PhaseEntry> phases;
+    void *rk_buf[4] = {nullptr, nullptr, nullptr, nullptr};  // RK: stage state, lapRot, NL term, sum
+    int *rk_lim = nullptr;    // RK: 2/3-rule limits per inner position (launch_mask_spectrum)
     cudaEvent_t ev[8] = {};
     int64_t launches = 0;
     int64_t bytes = 0;
@@ -185,9 +187,11 @@ static int upload_dw(gpss_ctx *c, void **dev, const std::vector<ldouble> &re, co
 }
 
 // Kinetic factor table for `axis` (splitting.jl:167/172/190/195/200):
-// real time  exp(i (cD xi^2 -/+ Om c xi) dtl), imaginary time exp((...) dtl);
-// fused tables also carry the 1/n of the inverse transform.  With Omega != 0
-// the x (y) table has one row per y (x) node.
+// real time  exp(i (cD xi^2 -/+ Om c xi) dtl), imaginary time exp((...) dtl),
+// imag == 2: the multiplier cD xi^2 -/+ Om c xi itself (the axis term of
+// lapRot, GrossPitaevskii.jl:12-45; dtl unused); fused tables also carry the
+// 1/n of the inverse transform.  With Omega != 0 the x (y) table has one row
+// per y (x) node.
 static int get_phase(gpss_ctx *c, int axis, double dtl, int imag, int fused, const void **dev,
                      int64_t *prow)
 {
@@ -215,7 +219,8 @@ static int get_phase(gpss_ctx *c, int axis, double dtl, int imag, int fused, con
             else if (axis == 1) ph = c->cD * (xk * xk) + c->omega * cr * xk;
             else ph = c->cD * (xk * xk);
             ldouble fr, fi;
-            if (!imag) { const ldouble t = (ldouble)(ph * dtl); fr = cosl(t); fi = sinl(t); }
+            if (imag == 2) { fr = (ldouble)ph; fi = 0.0L; }  // the multiplier itself (lapRot)
+            else if (!imag) { const ldouble t = (ldouble)(ph * dtl); fr = cosl(t); fi = sinl(t); }
             else { fr = expl((ldouble)(ph * dtl)); fi = 0.0L; }
             re[(size_t)(r * n + k)] = fr * inv_n;
             im[(size_t)(r * n + k)] = fi * inv_n;
@@ -287,7 +292,7 @@ static bool pipe_ok(const gpss_ctx *c, int axis)
 
 template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const PassArgs<T> &a)
 {
-    if (mode == MODE_FUSED && pipe_ok(c, axis)) {
+    if (mode == MODE_FUSED && !a.acc && pipe_ok(c, axis)) {
         const int ntiles = (int)(c->total / c->n[axis] / (4096 / c->n[axis]));
         cudaError_t e = PassLauncher<T>::pipe(axis == 0, (int)c->n[axis], a, ntiles, c->stream);
         if (e != cudaSuccess)
@@ -673,6 +678,124 @@ static int adjoint_impl(gpss_ctx *c, const double *psi_target, int nsteps, int K
     return GPSS_OK;
 }
 
+// ------------------------------------------------ explicit Runge-Kutta ----
+// timeStep!(::NumModelGPRK), explicit-rk.jl:135-166.  Every stage evaluates
+// gp_rhs! (:96-107): lapRot(q) as one fused pass per axis with the axis's
+// multiplier table (the x and y tables carry the rotation term per row),
+// accumulated across axes; the nonlinear term (V + beta|q|^2) q, 2/3-filtered
+// through the full transform (FWD passes, mask, INV passes) when filter is
+// "product"; then i (lapRot - N) goes straight into the stage state and the
+// running k1 + 2k2 + 2k3 + k4 sum.
+
+// largest kept |kk| along the last axis for every inner position, from the
+// reference's Float64 test (xi_x^2 + xi_y^2 [+ xi_z^2]) < xi_max
+static int rk_mask_table(gpss_ctx *c)
+{
+    if (c->rk_lim) return GPSS_OK;
+    double xmax = 0.0;
+    for (int a = 0; a < c->ndim; a++) {
+        double m = 0.0;
+        for (int64_t k = 0; k < c->n[a]; k++) {
+            const double x = xi_of(c, a, k);
+            if (x * x > m) m = x * x;
+        }
+        if (a == 0 || m < xmax) xmax = m;
+    }
+    xmax = (4.0 / 9.0) * xmax;  // Plans.jl:529-532
+    const int last = c->ndim - 1;
+    const int64_t inner = c->total / c->n[last], nl = c->n[last];
+    std::vector<int> lim((size_t)inner);
+    for (int64_t j = 0; j < inner; j++) {
+        const int64_t ix = j % c->n[0], iy = (j / c->n[0]) % c->n[1];
+        double sxy = xi_of(c, 0, ix) * xi_of(c, 0, ix);
+        if (c->ndim == 3) sxy = sxy + xi_of(c, 1, iy) * xi_of(c, 1, iy);
+        int best = -1;
+        for (int64_t kk = 0; kk <= nl / 2; kk++) {
+            const double z = (double)kk * xi_mult(c, last);
+            if (sxy + z * z < xmax) best = (int)kk;
+            else break;  // the test is monotone in |kk|
+        }
+        lim[(size_t)j] = best;
+    }
+    GPSS_TRY(dev_alloc(c, (void **)&c->rk_lim, lim.size() * sizeof(int)));
+    CUDA_TRY(c, cudaMemcpy(c->rk_lim, lim.data(), lim.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return GPSS_OK;
+}
+
+// in-place full transform of `f` (mul_all!/ldiv_all!): FWD x, y[, z] or INV z, y, x
+template <typename T> static int transform_all(gpss_ctx *c, void *f, bool inverse)
+{
+    for (int s = 0; s < c->ndim; s++) {
+        const int axis = inverse ? c->ndim - 1 - s : s;
+        PassArgs<T> a = axis_args<T>(c, axis, f, f);
+        GPSS_TRY(launch<T>(c, axis, inverse ? MODE_INV : MODE_FWD, a));
+    }
+    return GPSS_OK;
+}
+
+template <typename T> static int dealias_field(gpss_ctx *c, void *f)
+{
+    GPSS_TRY(rk_mask_table(c));
+    GPSS_TRY(transform_all<T>(c, f, false));
+    const int last = c->ndim - 1;
+    cudaError_t e = launch_mask_spectrum<T>((vec2<T> *)f, c->rk_lim, c->n[last], c->total / c->n[last], c->total,
+                                            c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "mask: %s", cudaGetErrorString(e));
+    c->launches++;
+    return transform_all<T>(c, f, true);
+}
+
+// k = i (lapRot(q) - N(q)) folded into the stage update (launch_rk_combine)
+template <typename T>
+static int rk_stage(gpss_ctx *c, const void *q, int filter, int acc_mode, double acc_w, double cf, int from_acc,
+                    void *out)
+{
+    void *k = c->rk_buf[1], *t = c->rk_buf[2], *acc = c->rk_buf[3];
+    for (int axis = 0; axis < c->ndim; axis++) {
+        PassArgs<T> a = axis_args<T>(c, axis, q, k);
+        const void *ph;
+        GPSS_TRY(get_phase(c, axis, 0.0, 2, 1, &ph, &a.prow));
+        a.phase = (const vec2<T> *)ph;
+        if (axis > 0) a.acc = (const vec2<T> *)k;
+        GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
+    }
+    cudaError_t e = launch_nl_term<T>((const vec2<T> *)q, c->have_V ? (const T *)c->V : nullptr, c->beta,
+                                      (vec2<T> *)t, c->total, c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl_term: %s", cudaGetErrorString(e));
+    c->launches++;
+    if (filter == 1) GPSS_TRY(dealias_field<T>(c, t));
+    e = launch_rk_combine<T>((const vec2<T> *)k, (const vec2<T> *)t, (const vec2<T> *)c->psi, (vec2<T> *)acc,
+                             (vec2<T> *)out, acc_mode, acc_w, cf, from_acc, c->total, c->stream);
+    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "rk_combine: %s", cudaGetErrorString(e));
+    c->launches++;
+    return GPSS_OK;
+}
+
+template <typename T> static int rk_step_impl(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
+{
+    const size_t fb = (size_t)c->total * sizeof(vec2<T>);
+    for (int i = 0; i < 4; i++)
+        if (!c->rk_buf[i]) GPSS_TRY(dev_alloc(c, &c->rk_buf[i], fb));
+    void *st = c->rk_buf[0];
+    const double half = 0.5 * dt, sixth = dt / 6;
+    for (int s = 0; s < nsteps; s++) {
+        if (stepper == 1) {
+            GPSS_TRY(rk_stage<T>(c, c->psi, filter, 0, 0.0, dt, 0, c->psi));
+        } else if (stepper == 2) {
+            GPSS_TRY(rk_stage<T>(c, c->psi, filter, 0, 0.0, half, 0, st));
+            GPSS_TRY(rk_stage<T>(c, st, filter, 0, 0.0, dt, 0, c->psi));
+        } else {
+            GPSS_TRY(rk_stage<T>(c, c->psi, filter, 1, 1.0, half, 0, st));
+            GPSS_TRY(rk_stage<T>(c, st, filter, 2, 2.0, half, 0, st));
+            GPSS_TRY(rk_stage<T>(c, st, filter, 2, 2.0, dt, 0, st));
+            GPSS_TRY(rk_stage<T>(c, st, filter, 2, 1.0, sixth, 1, c->psi));
+        }
+        if (filter == 2) GPSS_TRY(dealias_field<T>(c, c->psi));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GPSS_OK;
+}
+
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
 extern "C" {
@@ -693,7 +816,7 @@ void gpss_destroy(gpss_ctx *c)
     clear_phases(c);
     void *ptrs[] = {c->psi, c->scratch, c->V, c->tw[0], c->tw[1], c->tw[2], c->coord_dev[0],
                     c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status,
-                    c->counter};
+                    c->counter, c->rk_buf[0], c->rk_buf[1], c->rk_buf[2], c->rk_buf[3], c->rk_lim};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : c->ev)
@@ -867,6 +990,20 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
     if (nsteps == 0 && !diag) return GPSS_OK;
     if (c->precision == GPSS_FP32) return step_impl<float>(c, nsteps, scheme, imag, dt, diag);
     return step_impl<double>(c, nsteps, scheme, imag, dt, diag);
+}
+
+int gpss_rk_step(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "gpss_rk_step: no field uploaded");
+    if (nsteps < 0) return fail(c, GPSS_EINVAL, "gpss_rk_step: nsteps < 0");
+    if (stepper != 1 && stepper != 2 && stepper != 4)
+        return fail(c, GPSS_EINVAL, "gpss_rk_step: stepper must be 1, 2 or 4 (got %d)", stepper);
+    if (filter < 0 || filter > 2) return fail(c, GPSS_EINVAL, "gpss_rk_step: filter must be 0, 1 or 2");
+    if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "gpss_rk_step: dt must be finite");
+    cudaSetDevice(c->device);
+    return c->precision == GPSS_FP32 ? rk_step_impl<float>(c, nsteps, stepper, filter, dt)
+                                     : rk_step_impl<double>(c, nsteps, stepper, filter, dt);
 }
 
 int gpss_energy(gpss_ctx *c, double *out)

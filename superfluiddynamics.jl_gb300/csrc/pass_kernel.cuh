@@ -69,7 +69,8 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 // arguments; a leaner instantiation keeps fewer values live, which kept the
 // hot passes free of register spills under the 80-register bound):
 //   FEAT_NL    nonlinear epilogue and the mass sum
-//   FEAT_DIAG  energy sums (RED_POINT, RED_KIN), rotation (per-row phases)
+//   FEAT_DIAG  energy sums (RED_POINT, RED_KIN), rotation (per-row phases),
+//              accumulation into a second field
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3 };
 
 template <typename T> struct PassArgs {
@@ -107,6 +108,10 @@ template <typename T> struct PassArgs {
     double dV;
     T kmult;                 // xi_k = kk * kmult, kk the signed wavenumber index
     const double *coord;     // coordinate of each row (rotation energy), nullable
+    // FUSED: add the result to this field (same layout as out; may alias it) --
+    // the per-axis terms of a sum of directional operators (lapRot of the RK
+    // right-hand side); nullable
+    const vec2<T> *acc;
 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
@@ -568,8 +573,16 @@ pass_kernel(const PassArgs<T> a)
             }
         }
         if (valid) {
+            if (MODE == MODE_FUSED && kDiag && a.acc) {
 #pragma unroll
-            for (int j = 0; j < N1; j++) a.out[base + (uint32_t)(r + N2 * j) * st] = v[j];
+                for (int j = 0; j < N1; j++) {
+                    const uint32_t e = base + (uint32_t)(r + N2 * j) * st;
+                    a.out[e] = cadd(a.acc[e], v[j]);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < N1; j++) a.out[base + (uint32_t)(r + N2 * j) * st] = v[j];
+            }
         }
     } else if constexpr (MODE == MODE_FWD && N2 == 1) {
         if (valid) {

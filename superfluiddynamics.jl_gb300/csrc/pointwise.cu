@@ -104,6 +104,103 @@ cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaS
     return cudaGetLastError();
 }
 
+// ---- explicit Runge-Kutta (NumModelGPRK, explicit-rk.jl:96-166) ----
+
+// t = (V + beta |q|^2) q, the nonlinear term of gp_rhs! (explicit-rk.jl:100-106)
+template <typename T>
+__global__ void k_nl_term(const vec2<T> *__restrict__ q, const T *__restrict__ V, T beta, vec2<T> *__restrict__ t,
+                          int64_t total)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const vec2<T> v = q[e];
+        const T f = (V ? V[e] : (T)0) + beta * (v.x * v.x + v.y * v.y);
+        t[e] = mk<vec2<T>>(f * v.x, f * v.y);
+    }
+}
+
+template <typename T>
+cudaError_t launch_nl_term(const vec2<T> *q, const T *V, double beta, vec2<T> *t, int64_t total, cudaStream_t s)
+{
+    k_nl_term<T><<<grid_for(total, 256), 256, 0, s>>>(q, V, (T)beta, t, total);
+    return cudaGetLastError();
+}
+
+// 2/3-rule mask of a natural-order spectrum (_dealias_scalar!, NSGP.jl:354-361):
+// cell e has last-axis index e / inner; its signed wavenumber index kk is kept
+// iff |kk| <= lim[e % inner] (the host evaluates the reference's Float64 test
+// sum xi^2 < xi_max for every mode and stores the largest kept |kk| per
+// inner position, -1 for none).
+template <typename T>
+__global__ void k_mask_spectrum(vec2<T> *__restrict__ f, const int *__restrict__ lim, int64_t n_last, int64_t inner,
+                                int64_t total)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t il = e / inner;
+        const int64_t kk = il < (n_last + 1) / 2 ? il : n_last - il;
+        if (kk > lim[e % inner]) f[e] = mk<vec2<T>>((T)0, (T)0);
+    }
+}
+
+template <typename T>
+cudaError_t launch_mask_spectrum(vec2<T> *f, const int *lim, int64_t n_last, int64_t inner, int64_t total,
+                                 cudaStream_t s)
+{
+    k_mask_spectrum<T><<<grid_for(total, 256), 256, 0, s>>>(f, lim, n_last, inner, total);
+    return cudaGetLastError();
+}
+
+// One RK stage from k = lapRot(q) and t = the (filtered) nonlinear term:
+//   kk = i (k - t)                                  (gp_rhs!)
+//   acc_mode 1: acc = kk; 2: acc = acc + acc_w kk   (k1 + 2k2 + 2k3 + k4, left to right)
+//   out = psi0 + cf acc  (from_acc)  or  psi0 + cf kk
+template <typename T>
+__global__ void k_rk_combine(const vec2<T> *__restrict__ k, const vec2<T> *__restrict__ t, const vec2<T> *psi0,
+                             vec2<T> *acc, vec2<T> *out, int acc_mode, T acc_w, T cf, int from_acc, int64_t total)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const vec2<T> a = k[e], b = t[e];
+        const vec2<T> kk = mk<vec2<T>>(-(a.y - b.y), a.x - b.x);
+        vec2<T> s = kk;
+        if (acc_mode == 1) {
+            acc[e] = kk;
+        } else if (acc_mode == 2) {
+            const vec2<T> p = acc[e];
+            s = mk<vec2<T>>(p.x + acc_w * kk.x, p.y + acc_w * kk.y);
+            acc[e] = s;
+        }
+        const vec2<T> base = psi0[e];
+        const vec2<T> d = from_acc ? s : kk;
+        out[e] = mk<vec2<T>>(base.x + cf * d.x, base.y + cf * d.y);
+    }
+}
+
+template <typename T>
+cudaError_t launch_rk_combine(const vec2<T> *k, const vec2<T> *t, const vec2<T> *psi0, vec2<T> *acc, vec2<T> *out,
+                              int acc_mode, double acc_w, double cf, int from_acc, int64_t total, cudaStream_t s)
+{
+    k_rk_combine<T><<<grid_for(total, 256), 256, 0, s>>>(k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc,
+                                                         total);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_nl_term<float>(const vec2<float> *, const float *, double, vec2<float> *, int64_t,
+                                           cudaStream_t);
+template cudaError_t launch_nl_term<double>(const vec2<double> *, const double *, double, vec2<double> *, int64_t,
+                                            cudaStream_t);
+template cudaError_t launch_mask_spectrum<float>(vec2<float> *, const int *, int64_t, int64_t, int64_t,
+                                                 cudaStream_t);
+template cudaError_t launch_mask_spectrum<double>(vec2<double> *, const int *, int64_t, int64_t, int64_t,
+                                                  cudaStream_t);
+template cudaError_t launch_rk_combine<float>(const vec2<float> *, const vec2<float> *, const vec2<float> *,
+                                              vec2<float> *, vec2<float> *, int, double, double, int, int64_t,
+                                              cudaStream_t);
+template cudaError_t launch_rk_combine<double>(const vec2<double> *, const vec2<double> *, const vec2<double> *,
+                                               vec2<double> *, vec2<double> *, int, double, double, int, int64_t,
+                                               cudaStream_t);
+
 template cudaError_t launch_mul_phase<float>(vec2<float> *, const vec2<float> *, int64_t, int,
                                              const int64_t *, int64_t, cudaStream_t);
 template cudaError_t launch_mul_phase<double>(vec2<double> *, const vec2<double> *, int64_t, int,

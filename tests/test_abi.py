@@ -60,6 +60,7 @@ def test_null_arguments(L):
     assert L.gpss_create(None, 2, None, None, None, 64, 0) == -1
     assert L.gpss_set_params(None, 0, 0, 0) == -1
     assert L.gpss_step(None, 1, 2, 0, 1e-3, None) == -1
+    assert L.gpss_rk_step(None, 1, 4, 1, 1e-3) == -1
     L.gpss_destroy(None)
 
 
