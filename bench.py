@@ -24,6 +24,7 @@ JSON line keys beyond the base contract:
   accuracy       rel-L2 of the FP32 fused field vs the FP64 plain field.
   imag_time      cfg2: 128^3 imaginary-time steps, FP32 and FP64.
   adjoint        cfg4: one 2000-step gradient through gpss_adjoint.
+  rk4            the explicit RK4 integrator (NumModelGPRK) on the cfg1 field.
   cufft_comparison  the same directional pass through cuFFT (torch.fft).
 
 --impl reference times the CPU restatement of the reference path (the
@@ -329,6 +330,25 @@ def measure_adjoint(sfd, W):
     return out
 
 
+def measure_rk(sfd, c, L, steps=4):
+    """The explicit RK4 integrator (NumModelGPRK, 2/3 filter on the product) on
+    the cfg1 field at 256^3, FP32 and FP64, CUDA events around gpss_rk_step."""
+    cells = float(math.prod(c["shape"]))
+    out = {"workload": f"cfg1 field, 256^3, RK4, filter product, dt=1e-3, {steps} steps per timing"}
+    for prec in ("fp32", "fp64"):
+        grid = sfd.Grid(c["shape"], c["bounds"])
+        f = sfd.Field(grid)
+        f.phi = c["psi"]
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+        m = sfd.NumModelGPRK(f, p, 1e-3, steps, steps, stepper="RK4", filter="product", precision=prec)
+        h = m.handle
+        L.gpss_rk_step(h, 1, 4, 1, 1e-3)
+        ms = _event_ms(L, h, lambda: L.gpss_rk_step(h, steps, 4, 1, 1e-3))
+        out[prec] = {"value": cells * steps / (ms / 1e3) / 1e6, "unit": "Mcell-steps/s", "ms_per_step": ms / steps}
+        m.close(download=False)
+    return out
+
+
 def measure_cufft(c, n, reps=20):
     """The same directional pass (FFT -> phase multiply -> inverse FFT) through
     cuFFT (torch.fft, complex64) on the 256^3 field, per axis, for comparison."""
@@ -483,6 +503,7 @@ def run_gpss(args, rank, world, local):
         extra["accuracy"] = measure_accuracy(sfd, c)
         extra["imag_time"] = measure_imag(sfd, W, L)
         extra["adjoint"] = measure_adjoint(sfd, W)
+        extra["rk4"] = measure_rk(sfd, c, L)
         cu = measure_cufft(c, args.n)
         if cu:
             cu["gpss_pass_ms"] = per_axis
