@@ -352,3 +352,61 @@ def test_pipelined_pass_matches_direct_kernel(sfd, O, precision, shape):
         c = run_model(sfd, shape, bounds, psi0, pipeline=True, **dict(kw, masslock=True))
         d = run_model(sfd, shape, bounds, psi0, pipeline=False, **dict(kw, masslock=True))
         assert O.rel_l2(c, d) < 1e-6
+
+
+# ------------------------------------------------ FP32 coverage, every size --
+@pytest.mark.parametrize("shape,nd", SHAPES)
+def test_fp32_fused_shapes(sfd, O, shape, nd):
+    """Every line length 2..256 and both layouts in FP32 (lean and full
+    instantiations: trap potential and rotation), vs the FP64 oracle."""
+    bounds = tuple((-3.0 - a, 4.0 + 0.5 * a) for a in range(nd))
+    psi0 = random_field(shape, seed=7 + sum(shape))
+    V = O.quadratic_potential(shape, bounds, gammas=[1.0, 0.7, 1.3][:nd])
+    for omega in (0.0, 0.3):
+        kw = dict(coeffD=-0.5, beta=3.0, omega=omega, V=V, dt=2e-3, nsteps=5)
+        got = run_model(sfd, shape, bounds, psi0, precision="fp32", **kw)
+        ref = O.c_step(psi0, bounds, **kw)
+        assert O.rel_l2(got, ref) < TOL32
+
+
+# ------------------------------------------- full-size (256^3) properties --
+def test_fullsize_linear_flow_is_exact_fp32(sfd, O, W):
+    """beta = V = 0 at 256^3: every merged FP32 pass applies the exact kinetic
+    factor, so 20 steps equal exp(i coeffD |k|^2 t) on the spectrum (numpy
+    FFT in complex128 of the same input) to FP32 round-off."""
+    c = W.cfg1(256)
+    got = run_model(sfd, c["shape"], c["bounds"], c["psi"], coeffD=c["coeffD"], beta=0.0, dt=c["dt"],
+                    nsteps=20, precision="fp32")
+    F = np.fft.fftn(c["psi"])
+    k2 = 0
+    for a in range(3):
+        xi = np.fft.fftfreq(256, 2 * math.pi / 256) * 2 * math.pi
+        s = [1, 1, 1]
+        s[a] = 256
+        k2 = k2 + xi.reshape(s) ** 2
+    want = np.fft.ifftn(F * np.exp(1j * c["coeffD"] * k2 * (20 * c["dt"])))
+    assert O.rel_l2(got, want) < 3e-6
+
+
+def test_fullsize_time_reversal_fp32(sfd, O, W):
+    """Strang splitting is time-reversible: N(-dt) undoes N(dt) (it keeps
+    |psi|), the kinetic flows are unitary.  40 steps forward then 40 with -dt
+    at 256^3 in FP32 return the initial field to round-off, and the FP64
+    reductions see the mass and energy come back."""
+    c = W.cfg1(256)
+    g = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(g)
+    f.phi = c["psi"]
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+    n = sfd.NumModelSplit2(f, p, c["dt"], 1, 1, precision="fp32")
+    e0 = n.energies()
+    n.step(40)
+    mid = f.phi.copy()
+    n.dt = -c["dt"]
+    n.step(40)
+    back = f.phi.copy()
+    e1 = n.energies()
+    n.close()
+    assert O.rel_l2(mid, c["psi"]) > 1e-2          # the field did move
+    assert O.rel_l2(back, c["psi"]) < 1e-5
+    assert abs(e1[3] - e0[3]) < 1e-5 * abs(e0[3])
