@@ -51,7 +51,8 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
     switch (mode) {
     case MODE_FUSED: {
         // the leanest instantiation that does everything the arguments ask for
-        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr;
+        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr ||
+                          a.pre_out != nullptr || a.adj_pre != nullptr;
         const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
         if (diag) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
         if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NL>(a, blocks, s);

@@ -112,6 +112,15 @@ template <typename T> struct PassArgs {
     // the per-axis terms of a sum of directional operators (lapRot of the RK
     // right-hand side); nullable
     const vec2<T> *acc;
+    // FUSED with the NL epilogue: also store the value entering the NL stage
+    // here (the states the discrete adjoint needs); nullable
+    vec2<T> *pre_out;
+    // FUSED: replace the NL epilogue by its adjoint at the state adj_pre (the
+    // input of the forward NL stage; constants nl_beta/nl_dt/nl_split, V):
+    //   g <- conj(f) g + 2 beta dt Im(conj(g) f pre) pre,
+    //   adj_dLdV += dt Im(conj(g) f pre),   f = exp(-i (V + beta|pre|^2) dt)
+    const vec2<T> *adj_pre;
+    double *adj_dLdV;
 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
@@ -506,6 +515,28 @@ pass_kernel(const PassArgs<T> a)
 
     // ---- epilogue: positions r + N2 j
     if constexpr (MODE == MODE_FUSED || MODE == MODE_INV) {
+        if constexpr (MODE == MODE_FUSED && kDiag) {
+            if (a.pre_out && valid) {
+#pragma unroll
+                for (int j = 0; j < N1; j++) a.pre_out[base + (uint32_t)(r + N2 * j) * st] = v[j];
+            }
+            if (a.adj_pre) {
+                const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);
+                const T two_beta_dt = (T)(2.0 * a.nl_beta * a.nl_dt);
+#pragma unroll
+                for (int j = 0; j < N1; j++) {
+                    const uint32_t e = base + (uint32_t)(r + N2 * j) * st;
+                    const V pre = a.adj_pre[e];
+                    const T vv = a.V ? a.V[e] : (T)0;
+                    const V f = nl_factor(pre, vv, nlc, false);
+                    const V pout = nl_rotate(f, pre);
+                    const T im = v[j].x * pout.y - v[j].y * pout.x;  // Im(conj(g) psi_out)
+                    if (valid) a.adj_dLdV[e] += a.nl_dt * (double)im;
+                    const V rot = cmulc(v[j], f);                     // conj(f) g
+                    v[j] = mk<V>(rot.x + two_beta_dt * im * pre.x, rot.y + two_beta_dt * im * pre.y);
+                }
+            }
+        }
         if constexpr (MODE == MODE_FUSED) {
             if (kNL && a.nl_mode != NL_NONE) {
                 const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);

@@ -121,3 +121,34 @@ def test_adjoint_cfg4_full_size(sfd, O, W):
         assert abs(fd - adj) <= 1e-6 * abs(adj)
     assert abs(L32 - L64) < 1e-4
     assert np.linalg.norm(dV32 - dV64) / np.linalg.norm(dV64) < 1e-2
+
+
+def test_adjoint_with_rotation_vs_finite_differences(sfd, O, W):
+    """Omega != 0 (the x and y flows do not commute, so the unmerged
+    sequence is differentiated): dL/dV against central differences."""
+    c = W.cfg4(32)
+    nsteps, K = 30, 7
+    g = sfd.Grid(c["shape"], c["bounds"])
+
+    def model(V):
+        f = sfd.Field(g)
+        f.phi = c["psi"]
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=c["coeffD"], beta=c["beta"], Omega=0.4)
+        return f, sfd.NumModelSplit2(f, p, c["dt"], nsteps, nsteps, merge=False, masslock=False)
+
+    def loss(V):
+        f, n = model(V)
+        n.step(nsteps)
+        psi = f.phi.copy(order="F")
+        n.close()
+        dV = np.prod([(b[1] - b[0]) / m for m, b in zip(c["shape"], c["bounds"])])
+        return 1.0 - abs(np.sum(np.conj(c["target"]) * psi) * dV) ** 2
+
+    f, n = model(c["V"])
+    L, dLdV, _ = n.adjoint(c["target"], nsteps, K)
+    n.close()
+    assert abs(L - loss(c["V"])) < 1e-13
+    eps = 1e-4
+    for dv in _directions(c["shape"], 4, seed=13):
+        fd = (loss(c["V"] + eps * dv) - loss(c["V"] - eps * dv)) / (2 * eps)
+        assert abs(fd - float(np.sum(dLdV * dv))) <= 1e-6 * abs(fd)
