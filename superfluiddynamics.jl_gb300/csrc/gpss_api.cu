@@ -7,6 +7,7 @@
 #include <cstring>
 #include <algorithm>
 #include <new>
+#include <string>
 #include "../../include/gpss.h"
 #include "gpss_internal.h"
 
@@ -53,6 +54,13 @@ struct gpss_ctx {
     // discrete adjoint: buffers kept between calls (sized for adj_nck checkpoints, adj_K states)
     void *adj_buf = nullptr;
     size_t adj_bytes = 0;
+    // CUDA graphs of repeated launch sequences (graph_run), keyed by what they bake in
+    struct GraphEntry {
+        std::string key;
+        cudaGraphExec_t exec = nullptr;  // null: seen once, captured on the next call
+        int64_t launches = 0;
+    };
+    std::vector<GraphEntry> graphs;
     cudaEvent_t ev[8] = {};
     int64_t launches = 0;
     int64_t bytes = 0;
@@ -189,6 +197,8 @@ static int upload_dw(gpss_ctx *c, void **dev, const std::vector<ldouble> &re, co
     return GPSS_OK;
 }
 
+static void clear_graphs(gpss_ctx *c);
+
 // Kinetic factor table for `axis` (splitting.jl:167/172/190/195/200):
 // real time  exp(i (cD xi^2 -/+ Om c xi) dtl), imaginary time exp((...) dtl),
 // imag == 2: the multiplier cD xi^2 -/+ Om c xi itself (the axis term of
@@ -232,6 +242,7 @@ static int get_phase(gpss_ctx *c, int axis, double dtl, int imag, int fused, con
     PhaseEntry e{axis, imag, fused, dtl, c->cD, c->omega, nullptr, rot ? 2 * n : 0};
     GPSS_TRY(upload_dw(c, &e.dev, re, im, rows, n));
     if (c->phases.size() > 64) {  // bounded cache: drop the oldest
+        clear_graphs(c);
         cudaStreamSynchronize(c->stream);
         cudaFree(c->phases.front().dev);
         c->phases.erase(c->phases.begin());
@@ -242,12 +253,82 @@ static int get_phase(gpss_ctx *c, int axis, double dtl, int imag, int fused, con
     return GPSS_OK;
 }
 
+// Graphs hold kernel arguments (table and buffer pointers, beta, V): any change
+// of those drops them.
+static void clear_graphs(gpss_ctx *c)
+{
+    if (c->graphs.empty()) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &e : c->graphs)
+        if (e.exec) cudaGraphExecDestroy(e.exec);
+    c->graphs.clear();
+}
+
 static void clear_phases(gpss_ctx *c)
 {
+    clear_graphs(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &e : c->phases) cudaFree(e.dev);
     c->phases.clear();
 }
+
+// Run a launch sequence that is issued repeatedly with the same arguments: the
+// first time eagerly (which also creates its tables and kernel attributes),
+// the second time captured into a CUDA graph, afterwards by launching the
+// graph.  Small fields spend most of a step in launch overhead; a graph
+// replays the sequence with back-to-back kernels.
+template <typename F> static int graph_run(gpss_ctx *c, const std::string &key, F issue)
+{
+    for (auto &e : c->graphs) {
+        if (e.key != key) continue;
+        if (e.exec) {
+            CUDA_TRY(c, cudaGraphLaunch(e.exec, c->stream));
+            c->launches += e.launches;
+            return GPSS_OK;
+        }
+        const int64_t l0 = c->launches;
+        CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = issue();
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+        if (rc != GPSS_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ee != cudaSuccess) return fail(c, GPSS_ECUDA, "graph capture: %s", cudaGetErrorString(ee));
+        const cudaError_t ie = cudaGraphInstantiate(&e.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            e.exec = nullptr;
+            return fail(c, GPSS_ECUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+        }
+        e.launches = c->launches - l0;
+        CUDA_TRY(c, cudaGraphLaunch(e.exec, c->stream));
+        return GPSS_OK;
+    }
+    if (c->graphs.size() >= 16) {
+        cudaStreamSynchronize(c->stream);
+        if (c->graphs.front().exec) cudaGraphExecDestroy(c->graphs.front().exec);
+        c->graphs.erase(c->graphs.begin());
+    }
+    c->graphs.push_back(gpss_ctx::GraphEntry{key, nullptr, 0});
+    return issue();
+}
+
+static std::string graph_key(const char *what, std::initializer_list<double> v)
+{
+    std::string k(what);
+    char buf[40];
+    for (double x : v) {
+        snprintf(buf, sizeof(buf), ":%a", x);
+        k += buf;
+    }
+    return k;
+}
+
+// fields up to this many cells replay their repeated step sequences from CUDA graphs
+static const int64_t kGraphCells = int64_t(1) << 21;
+static const int kGraphChunk = 32;  // time steps per captured chunk
 
 template <typename T> static PassArgs<T> axis_args(gpss_ctx *c, int axis, const void *in, void *out)
 {
@@ -517,7 +598,17 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         // L(dt/2) N [L(dt) N]^(nsteps-1) L(dt/2): the kinetic flows of
         // consecutive steps commute (Omega = 0) and compose exactly.
         GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, red_nl, false, false, fin_nl));
-        for (int s = 1; s < nsteps; s++)
+        int s = 1;
+        if (c->total <= kGraphCells) {
+            const std::string key = graph_key("step", {dt, (double)lock, (double)kGraphChunk});
+            for (; s + kGraphChunk <= nsteps; s += kGraphChunk)
+                GPSS_TRY(graph_run(c, key, [&]() -> int {
+                    for (int i = 0; i < kGraphChunk; i++)
+                        GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, red_nl, false, lock, fin_nl));
+                    return GPSS_OK;
+                }));
+        }
+        for (; s < nsteps; s++)
             GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, red_nl, false, lock, fin_nl));
         // final half step; with diag, the kinetic sums of each axis are exact
         // for the final field (real-time kinetic flows are unitary and commute
@@ -652,6 +743,7 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
     const size_t red_bytes = sizeof(double) * (2 * 152 * 8 + 2);
     const size_t need = fb * (size_t)(4 + K + nck) + (size_t)c->total * sizeof(double) + red_bytes;
     if (c->adj_bytes < need) {
+        clear_graphs(c);
         if (c->adj_buf) { cudaStreamSynchronize(c->stream); cudaFree(c->adj_buf); c->adj_buf = nullptr; c->adj_bytes = 0; }
         GPSS_TRY(dev_alloc(c, &c->adj_buf, need));
         c->adj_bytes = need;
@@ -664,8 +756,6 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
     double *red = dv + c->total;
     double *zdev = red + 2 * 152 * 8;
     const double dV = cell_volume(c), h = dt * 0.5;
-    CUDA_TRY(c, cudaMemcpyAsync(psi0, c->psi, fb, cudaMemcpyDeviceToDevice, c->stream));
-    CUDA_TRY(c, cudaMemsetAsync(dv, 0, (size_t)c->total * sizeof(double), c->stream));
     if (c->precision == GPSS_FP64) {
         CUDA_TRY(c, cudaMemcpyAsync(tgt, psi_target, fb, cudaMemcpyHostToDevice, c->stream));
     } else {
@@ -673,37 +763,46 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
                                     c->stream));
         CUDA_TRY(c, launch_f64_to_f32((const double *)c->scratch, (float *)tgt, 2 * c->total, c->stream));
     }
-    // forward: c->psi becomes N(pre_n) after group n; pre_n kept at the checkpoints
-    for (int n = 0; n < nsteps; n++)
-        GPSS_TRY(adj_group<T>(c, c->psi, n == 0 ? h : dt, false, true, dt, n % K == 0 ? ckpt(n / K) : nullptr,
-                              nullptr, nullptr));
-    GPSS_TRY(adj_group<T>(c, c->psi, h, false, false, 0.0, nullptr, nullptr, nullptr));
-    // loss and the adjoint of the final field
-    CUDA_TRY(c, launch_overlap<T>((const V *)tgt, (const V *)c->psi, c->total, red, dV, zdev, c->stream));
+    // everything from here to the outputs is device work with fixed arguments:
+    // a repeated call replays it as one CUDA graph
+    auto body = [&]() -> int {
+        CUDA_TRY(c, cudaMemcpyAsync(psi0, c->psi, fb, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(c, cudaMemsetAsync(dv, 0, (size_t)c->total * sizeof(double), c->stream));
+        // forward: c->psi becomes N(pre_n) after group n; pre_n kept at the checkpoints
+        for (int n = 0; n < nsteps; n++)
+            GPSS_TRY(adj_group<T>(c, c->psi, n == 0 ? h : dt, false, true, dt, n % K == 0 ? ckpt(n / K) : nullptr,
+                                  nullptr, nullptr));
+        GPSS_TRY(adj_group<T>(c, c->psi, h, false, false, 0.0, nullptr, nullptr, nullptr));
+        // loss and the adjoint of the final field
+        CUDA_TRY(c, launch_overlap<T>((const V *)tgt, (const V *)c->psi, c->total, red, dV, zdev, c->stream));
+        CUDA_TRY(c, launch_seed<T>((V *)g, (const V *)tgt, zdev, dV, c->total, c->stream));
+        c->launches += 3;
+        // backward, segment by segment from the last
+        for (int seg = nck - 1; seg >= 0; seg--) {
+            const int start = seg * K, end = std::min(start + K, nsteps);
+            if (end - start > 1) {
+                // work = N(pre_start), then pre_{start+j} = L(dt) N(pre_{start+j-1}) into state(j)
+                CUDA_TRY(c, cudaMemcpyAsync(work, ckpt(seg), fb, cudaMemcpyDeviceToDevice, c->stream));
+                cudaError_t e = launch_nl<T>((V *)work, c->have_V ? (const T *)c->V : nullptr, c->beta, dt, 0,
+                                             c->total, c->stream);
+                if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl: %s", cudaGetErrorString(e));
+                c->launches++;
+                for (int j = 1; j < end - start; j++)
+                    GPSS_TRY(adj_group<T>(c, work, dt, false, true, dt, state(j), nullptr, nullptr));
+            }
+            for (int n = end - 1; n >= start; n--) {
+                const void *pre = n == start ? ckpt(seg) : state(n - start);
+                GPSS_TRY(adj_group<T>(c, g, n == nsteps - 1 ? -h : -dt, true, false, dt, nullptr, pre, dv));
+            }
+        }
+        GPSS_TRY(adj_group<T>(c, g, -h, true, false, 0.0, nullptr, nullptr, nullptr));
+        CUDA_TRY(c, cudaMemcpyAsync(c->psi, psi0, fb, cudaMemcpyDeviceToDevice, c->stream));
+        return GPSS_OK;
+    };
+    GPSS_TRY(graph_run(c, graph_key("adjoint", {(double)nsteps, (double)K, dt, (double)c->have_V}), body));
     double z[2];
     CUDA_TRY(c, cudaMemcpyAsync(z, zdev, sizeof(z), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, launch_seed<T>((V *)g, (const V *)tgt, zdev, dV, c->total, c->stream));
-    c->launches += 3;
-    // backward, segment by segment from the last
-    for (int seg = nck - 1; seg >= 0; seg--) {
-        const int start = seg * K, end = std::min(start + K, nsteps);
-        if (end - start > 1) {
-            // work = N(pre_start), then pre_{start+j} = L(dt) N(pre_{start+j-1}) into state(j)
-            CUDA_TRY(c, cudaMemcpyAsync(work, ckpt(seg), fb, cudaMemcpyDeviceToDevice, c->stream));
-            cudaError_t e = launch_nl<T>((V *)work, c->have_V ? (const T *)c->V : nullptr, c->beta, dt, 0, c->total,
-                                         c->stream);
-            if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl: %s", cudaGetErrorString(e));
-            c->launches++;
-            for (int j = 1; j < end - start; j++)
-                GPSS_TRY(adj_group<T>(c, work, dt, false, true, dt, state(j), nullptr, nullptr));
-        }
-        for (int n = end - 1; n >= start; n--) {
-            const void *pre = n == start ? ckpt(seg) : state(n - start);
-            GPSS_TRY(adj_group<T>(c, g, n == nsteps - 1 ? -h : -dt, true, false, dt, nullptr, pre, dv));
-        }
-    }
-    GPSS_TRY(adj_group<T>(c, g, -h, true, false, 0.0, nullptr, nullptr, nullptr));
-    // outputs; the context's field goes back to the initial state
+    // outputs; the context's field is back at the initial state
     if (dLdV) CUDA_TRY(c, cudaMemcpyAsync(dLdV, dv, (size_t)c->total * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (dLdpsi0) {
         if (c->precision == GPSS_FP64) {
@@ -714,7 +813,6 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
                                         c->stream));
         }
     }
-    CUDA_TRY(c, cudaMemcpyAsync(c->psi, psi0, fb, cudaMemcpyDeviceToDevice, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     *loss = 1.0 - (z[0] * z[0] + z[1] * z[1]);
     if (!std::isfinite(*loss)) return fail(c, GPSS_ENONFINITE, "adjoint: non-finite loss");
@@ -905,7 +1003,7 @@ template <typename T> static int rk_step_impl(gpss_ctx *c, int nsteps, int stepp
         if (!c->rk_buf[i]) GPSS_TRY(dev_alloc(c, &c->rk_buf[i], fb));
     void *st = c->rk_buf[0];
     const double half = 0.5 * dt, sixth = dt / 6;
-    for (int s = 0; s < nsteps; s++) {
+    auto one_step = [&]() -> int {
         if (stepper == 1) {
             GPSS_TRY(rk_stage<T>(c, c->psi, filter, 0, 0.0, dt, 0, c->psi));
         } else if (stepper == 2) {
@@ -918,7 +1016,19 @@ template <typename T> static int rk_step_impl(gpss_ctx *c, int nsteps, int stepp
             GPSS_TRY(rk_stage<T>(c, st, filter, 2, 1.0, sixth, 1, c->psi));
         }
         if (filter == 2) GPSS_TRY(dealias_field<T>(c, c->psi));
+        return GPSS_OK;
+    };
+    int s = 0;
+    if (c->total <= kGraphCells) {
+        const int chunk = kGraphChunk / 4;
+        const std::string key = graph_key("rk", {(double)stepper, (double)filter, dt, (double)chunk});
+        for (; s + chunk <= nsteps; s += chunk)
+            GPSS_TRY(graph_run(c, key, [&]() -> int {
+                for (int i = 0; i < chunk; i++) GPSS_TRY(one_step());
+                return GPSS_OK;
+            }));
     }
+    for (; s < nsteps; s++) GPSS_TRY(one_step());
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return GPSS_OK;
 }
@@ -940,7 +1050,7 @@ void gpss_destroy(gpss_ctx *c)
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    clear_phases(c);
+    clear_phases(c);  // and the graphs
     void *ptrs[] = {c->psi, c->scratch, c->V, c->tw[0], c->tw[1], c->tw[2], c->coord_dev[0],
                     c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status,
                     c->counter, c->rk_buf[0], c->rk_buf[1], c->rk_buf[2], c->rk_buf[3], c->rk_lim,
@@ -1048,6 +1158,7 @@ int gpss_set_params(gpss_ctx *c, double coeffD, double beta, double omega)
         return fail(c, GPSS_EINVAL, "parameters must be finite");
     CUDA_TRY(c, cudaSetDevice(c->device));
     if (coeffD != c->cD || omega != c->omega) clear_phases(c);
+    clear_graphs(c);
     c->cD = coeffD;
     c->beta = beta;
     c->omega = omega;
@@ -1058,6 +1169,7 @@ int gpss_set_potential(gpss_ctx *c, const double *V)
 {
     if (!c) return GPSS_EINVAL;
     CUDA_TRY(c, cudaSetDevice(c->device));
+    clear_graphs(c);
     if (!V) { c->have_V = false; return GPSS_OK; }
     if (!c->V) GPSS_TRY(dev_alloc(c, &c->V, (size_t)c->total * real_bytes(c)));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
