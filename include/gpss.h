@@ -120,6 +120,29 @@ int gpss_step(gpss_ctx *ctx, int nsteps, int scheme, int imag, double dt, gpss_d
 int gpss_rk_step(gpss_ctx *ctx, int nsteps, int stepper, int filter, double dt);
 
 /*
+ * nsteps of an implicit scheme of size dt, solving its linear systems with
+ * the reference's BiCGStab (krylov!/krylovPreCond!, src/NumModels/krylov.jl:1-67;
+ * nkrylov iterations at most, relative residual tolkrylov).  Replaces timeStep! of
+ *   GPSS_IMPLICIT_BE          NumModelBackwardEuler            backward-euler.jl:62-83
+ *   GPSS_IMPLICIT_BE_NOPRE    NumModelBackwardEulerNoPrecond   backward-euler.jl:155-172
+ *   GPSS_IMPLICIT_CN          NumModelCrankNicolson            crank-nicolson.jl:62-103
+ *   GPSS_IMPLICIT_CN_QN       NumModelCrankNicolsonQuasiNewton crank-nicolson.jl:186-225
+ *   GPSS_IMPLICIT_CN_T        NumModelCrankNicolsonT           crank-nicolson.jl:308-347
+ *   GPSS_IMPLICIT_CN_QN_T     NumModelCrankNicolsonQuasiNewtonT crank-nicolson.jl:432-468
+ * (the CN schemes iterate Newton at most nnewton times to tolnewton; all but
+ * the T schemes renormalise to unit mass).  krylov_iters (nullable) receives
+ * the sum of the Krylov counts timeStep! returns.
+ */
+#define GPSS_IMPLICIT_BE 0
+#define GPSS_IMPLICIT_BE_NOPRE 1
+#define GPSS_IMPLICIT_CN 2
+#define GPSS_IMPLICIT_CN_QN 3
+#define GPSS_IMPLICIT_CN_T 4
+#define GPSS_IMPLICIT_CN_QN_T 5
+int gpss_implicit_step(gpss_ctx *ctx, int nsteps, int scheme, double dt, int nkrylov, double tolkrylov,
+                       int nnewton, double tolnewton, int64_t *krylov_iters);
+
+/*
  * Energies of the current field: out = {E_Omega, E_Delta, E_beta, E, mu}.
  * Replaces energy(n) (src/NumModels/GrossPitaevskii/GrossPitaevskii.jl:61-92 2D,
  * 106-136 3D; the 3D method prints no mu, the 2D formula is used for it).

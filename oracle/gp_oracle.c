@@ -22,6 +22,8 @@
  *                   RK1/RK2/RK4, 2/3-rule filter on the nonlinear term or the state),
  *                   lapRot GrossPitaevskii.jl:12-45, xi_max Plans.jl:529-532,
  *                   _dealias_scalar! NavierStokes/NSGP.jl:354-361
+ *   implicit        src/NumModels/GrossPitaevskii/backward-euler.jl, crank-nicolson.jl
+ *                   (six schemes) with BiCGStab src/NumModels/krylov.jl:1-67
  *   imaginary time  extension (no split-step counterpart in the reference): the
  *                   same stages with t -> -i tau and a unit-mass renormalisation
  *                   (normalize!, Fields.jl:196-200) after every step.
@@ -838,6 +840,252 @@ int OR_SYM(or_rk_step)(int ndim, const int64_t *n, const double *lo, const doubl
     for (int a = 0; a < 2; a++) free(c.rr[a]);
     for (int a = 0; a < 4; a++) free(k[a]);
     free(c.nl); free(st); free(p); free(Vr);
+    grid_free(&g);
+    return rc;
+}
+
+/* -------------------------------------- implicit imaginary-time schemes -- */
+
+/* lapRot(x) = -cD (ddx + ddy [+ ddz]) + (Om i)(rx + ry), GrossPitaevskii.jl:12-45 */
+static void lap_rot(const ogrid *g, const ocplx *x, real cD, real Om, ocplx **dd, ocplx **rr, ocplx *out)
+{
+    ocplx *d2[3] = {dd[0], g->ndim > 1 ? dd[1] : NULL, g->ndim > 2 ? dd[2] : NULL};
+    ocplx *r2[3] = {rr[0], g->ndim > 1 ? rr[1] : NULL, NULL};
+    ocplx *d1[3] = {NULL, NULL, NULL};
+    derivatives(g, x, d1, d2, r2);
+    int64_t N = g->total;
+    const real mcD = -cD;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        ocplx lap = dd[0][i];
+        if (g->ndim > 1) { lap.re = lap.re + dd[1][i].re; lap.im = lap.im + dd[1][i].im; }
+        if (g->ndim > 2) { lap.re = lap.re + dd[2][i].re; lap.im = lap.im + dd[2][i].im; }
+        ocplx rot = rr[0][i];
+        if (g->ndim > 1) { rot.re = rot.re + rr[1][i].re; rot.im = rot.im + rr[1][i].im; }
+        out[i].re = mcD * lap.re - Om * rot.im;
+        out[i].im = mcD * lap.im + Om * rot.re;
+    }
+}
+
+/* the six implicit schemes (backward-euler.jl, crank-nicolson.jl) */
+enum { IM_BE = 0, IM_BE_NOPRE = 1, IM_CN = 2, IM_CN_QN = 3, IM_CN_T = 4, IM_CN_QN_T = 5 };
+
+typedef struct {
+    const ogrid *g;
+    int scheme;
+    real cD, Om, idt;      /* idt = 1 / dt (Float64, as 1 / n.dt) */
+    ocplx *M;              /* real for BE / CN / CN_QN (im = 0), complex for the T schemes */
+    real *Anl;
+    ocplx *Anl2;
+    ocplx *b;
+    ocplx *dd[3], *rr[2], *lap;
+} im_ctx;
+
+/* prodA of each scheme (backward-euler.jl:87-90, 179-189; crank-nicolson.jl:112-114,
+ * 234-236, 356-359, 478-481) */
+static void prodA(im_ctx *c, const ocplx *x, ocplx *out)
+{
+    const ogrid *g = c->g;
+    lap_rot(g, x, c->cD, c->Om, c->dd, c->rr, c->lap);
+    int64_t N = g->total;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        const ocplx v = x[i], L = c->lap[i];
+        ocplx o;
+        switch (c->scheme) {
+        case IM_BE:       /* x - M lapRot(x) */
+            o.re = v.re - c->M[i].re * L.re; o.im = v.im - c->M[i].re * L.im; break;
+        case IM_BE_NOPRE: { /* (1/dt + Anl) x - lapRot(x) */
+            real a = c->idt + c->Anl[i];
+            o.re = a * v.re - L.re; o.im = a * v.im - L.im; break; }
+        case IM_CN: {     /* (1/dt + Anl) x + 0.5 Anl2 conj(x) - 0.5 lapRot(x) */
+            real a = c->idt + c->Anl[i];
+            ocplx h = {(real)0.5 * c->Anl2[i].re, (real)0.5 * c->Anl2[i].im};
+            /* h * conj(v) */
+            real hr = h.re * v.re + h.im * v.im, hi = h.im * v.re - h.re * v.im;
+            o.re = a * v.re + hr - (real)0.5 * L.re; o.im = a * v.im + hi - (real)0.5 * L.im; break; }
+        case IM_CN_QN: {  /* (1/dt + 0.5 Anl) x - 0.5 lapRot(x) */
+            real a = c->idt + c->Anl[i] * (real)0.5;
+            o.re = a * v.re - (real)0.5 * L.re; o.im = a * v.im - (real)0.5 * L.im; break; }
+        case IM_CN_T: {   /* (i/dt - 0.5 Anl) x - 0.5 Anl2 conj(x) + 0.5 lapRot(x) */
+            real ar = -(real)0.5 * c->Anl[i], ai = c->idt;
+            ocplx h = {(real)0.5 * c->Anl2[i].re, (real)0.5 * c->Anl2[i].im};
+            real hr = h.re * v.re + h.im * v.im, hi = h.im * v.re - h.re * v.im;
+            o.re = (ar * v.re - ai * v.im) - hr + (real)0.5 * L.re;
+            o.im = (ar * v.im + ai * v.re) - hi + (real)0.5 * L.im; break; }
+        default: {        /* IM_CN_QN_T: (i/dt - 0.5 Anl) x + 0.5 lapRot(x) */
+            real ar = -(c->Anl[i] * (real)0.5), ai = c->idt;
+            o.re = (ar * v.re - ai * v.im) + (real)0.5 * L.re;
+            o.im = (ar * v.im + ai * v.re) + (real)0.5 * L.im; break; }
+        }
+        out[i] = o;
+    }
+}
+
+static real re_dot(const ogrid *g, const ocplx *a, const ocplx *b, real *tmp)
+{
+    int64_t N = g->total;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) tmp[i] = a[i].re * b[i].re + a[i].im * b[i].im;
+    return pairwise_sum(tmp, N);
+}
+
+static void cmul_field(const ogrid *g, const ocplx *M, ocplx *x)
+{
+    int64_t N = g->total;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+        real xr = M[i].re * x[i].re - M[i].im * x[i].im, xi = M[i].re * x[i].im + M[i].im * x[i].re;
+        x[i].re = xr; x[i].im = xi;
+    }
+}
+
+/* BiCGStab, krylov! (precond = 0) and krylovPreCond! (precond = 1), krylov.jl:1-67;
+ * returns the iteration count of the reference (the last completed iteration
+ * before the convergence test passes) */
+static int krylov_solve(im_ctx *c, ocplx *phi, int nkrylov, real tol, int precond, ocplx **w, real *tmp)
+{
+    const ogrid *g = c->g;
+    int64_t N = g->total;
+    ocplx *r = w[0], *r2 = w[1], *p = w[2], *Ap = w[3], *s = w[4], *As = w[5];
+    if (precond) {
+        for (int64_t i = 0; i < N; i++) s[i] = c->b[i];
+        cmul_field(g, c->M, s);
+    }
+    const real normb = RSQRT(re_dot(g, precond ? s : c->b, precond ? s : c->b, tmp));
+    prodA(c, phi, r);
+    for (int64_t i = 0; i < N; i++) { r[i].re = c->b[i].re - r[i].re; r[i].im = c->b[i].im - r[i].im; }
+    if (precond) cmul_field(g, c->M, r);
+    for (int64_t i = 0; i < N; i++) { r2[i] = r[i]; p[i] = r[i]; }
+    int niter = 0;
+    for (int it = 1; it <= nkrylov; it++) {
+        prodA(c, p, Ap);
+        if (precond) cmul_field(g, c->M, Ap);
+        real rr2 = re_dot(g, r, r2, tmp), Apr2 = re_dot(g, Ap, r2, tmp);
+        real alpha = rr2 / Apr2;
+        for (int64_t i = 0; i < N; i++) { s[i].re = r[i].re - alpha * Ap[i].re; s[i].im = r[i].im - alpha * Ap[i].im; }
+        prodA(c, s, As);
+        if (precond) cmul_field(g, c->M, As);
+        real Ass = re_dot(g, As, s, tmp), AsAs = re_dot(g, As, As, tmp);
+        real omega = Ass / AsAs;
+        for (int64_t i = 0; i < N; i++) {
+            phi[i].re = (phi[i].re + alpha * p[i].re) + omega * s[i].re;
+            phi[i].im = (phi[i].im + alpha * p[i].im) + omega * s[i].im;
+        }
+        real rr2old = re_dot(g, r, r2, tmp);
+        for (int64_t i = 0; i < N; i++) { r[i].re = s[i].re - omega * As[i].re; r[i].im = s[i].im - omega * As[i].im; }
+        real rr = re_dot(g, r, r, tmp);
+        if (RSQRT(rr) / normb < tol) break;
+        niter = it;
+        rr2 = re_dot(g, r, r2, tmp);
+        real beta = rr2 / rr2old * alpha / omega;
+        for (int64_t i = 0; i < N; i++) {
+            real qr = p[i].re - omega * Ap[i].re, qi = p[i].im - omega * Ap[i].im;
+            p[i].re = r[i].re + beta * qr; p[i].im = r[i].im + beta * qi;
+        }
+    }
+    return niter;
+}
+
+/*
+ * nsteps of one implicit scheme: scheme IM_BE (NumModelBackwardEuler,
+ * backward-euler.jl:62-83), IM_BE_NOPRE (NumModelBackwardEulerNoPrecond,
+ * :155-172), IM_CN / IM_CN_QN / IM_CN_T / IM_CN_QN_T (NumModelCrankNicolson*,
+ * crank-nicolson.jl:62-103, 186-225, 308-347, 432-468: Newton loop of
+ * nnewton iterations to tolnewton around a preconditioned BiCGStab; the
+ * stationary schemes renormalise with normalize!, the T schemes do not).
+ * kry_total receives the sum of the returned Krylov counts.
+ */
+int OR_SYM(or_implicit_step)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                             double cD, double beta, double Om, const double *V, double *psi,
+                             int nsteps, int scheme, double dt, int nkrylov, double tolkrylov,
+                             int nnewton, double tolnewton, int64_t *kry_total)
+{
+    if (scheme < 0 || scheme > 5) return -1;
+    ogrid g;
+    if (grid_make(&g, ndim, n, lo, hi)) return -1;
+    int64_t N = g.total;
+    im_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.g = &g; c.scheme = scheme; c.cD = (real)cD; c.Om = (real)Om; c.idt = (real)(1.0 / dt);
+    ocplx *p = load_field(psi, N);
+    real *Vr = load_real(V, N);
+    ocplx *w[6] = {0}, *psim = NULL, *phi1 = NULL, *phiw = NULL;
+    real *tmp = (real *)malloc(sizeof(real) * (size_t)N);
+    int rc = (p && (!V || Vr) && tmp) ? 0 : -1;
+    ocplx **allc[] = {&c.M, &c.Anl2, &c.b, &c.dd[0], &c.dd[1], &c.dd[2], &c.rr[0], &c.rr[1], &c.lap,
+                      &w[0], &w[1], &w[2], &w[3], &w[4], &w[5], &psim, &phi1, &phiw};
+    for (size_t i = 0; rc == 0 && i < sizeof(allc) / sizeof(allc[0]); i++)
+        if (!(*allc[i] = (ocplx *)calloc((size_t)N, sizeof(ocplx)))) rc = -1;
+    if (rc == 0 && !(c.Anl = (real *)calloc((size_t)N, sizeof(real)))) rc = -1;
+    const real rbeta = (real)beta, rdt = (real)dt;
+    int64_t ktot = 0;
+    for (int st = 0; rc == 0 && st < nsteps; st++) {
+        if (scheme == IM_BE || scheme == IM_BE_NOPRE) {
+            for (int64_t i = 0; i < N; i++) {
+                real vv = Vr ? Vr[i] : 0, a2 = p[i].re * p[i].re + p[i].im * p[i].im;
+                if (scheme == IM_BE) {
+                    real m = (real)1.0 / ((real)1 / rdt + vv + rbeta * a2);
+                    c.M[i].re = m; c.M[i].im = 0;
+                    c.b[i].re = m * p[i].re / rdt; c.b[i].im = m * p[i].im / rdt;
+                } else {
+                    c.Anl[i] = vv + rbeta * a2;
+                    c.b[i].re = p[i].re / rdt; c.b[i].im = p[i].im / rdt;
+                }
+            }
+            ktot += krylov_solve(&c, p, nkrylov, (real)tolkrylov, 0, w, tmp);
+            real nrm = field_norm(&g, p);
+            for (int64_t i = 0; i < N; i++) { p[i].re /= nrm; p[i].im /= nrm; }
+            continue;
+        }
+        const int tsch = scheme == IM_CN_T || scheme == IM_CN_QN_T;
+        const int newton = scheme == IM_CN || scheme == IM_CN_T;
+        for (int64_t i = 0; i < N; i++) { phi1[i] = p[i]; phiw[i].re = 0; phiw[i].im = 0; }
+        for (int itn = 1; itn <= nnewton; itn++) {
+            for (int64_t i = 0; i < N; i++) {
+                psim[i].re = (real)0.5 * (phi1[i].re + p[i].re);
+                psim[i].im = (real)0.5 * (phi1[i].im + p[i].im);
+                real vv = Vr ? Vr[i] : 0, a2 = psim[i].re * psim[i].re + psim[i].im * psim[i].im;
+                c.Anl[i] = newton ? vv + 2 * rbeta * a2 : vv + 3 * rbeta * a2;
+                /* beta * psi * psi */
+                real qr = rbeta * psim[i].re, qi = rbeta * psim[i].im;
+                c.Anl2[i].re = qr * psim[i].re - qi * psim[i].im;
+                c.Anl2[i].im = qr * psim[i].im + qi * psim[i].re;
+                real d = (vv + 3 * rbeta * a2) * (real)0.5;
+                if (!tsch) { c.M[i].re = (real)1.0 / ((real)1.0 / rdt + d); c.M[i].im = 0; }
+                else {       /* 1 / (i/dt - d) */
+                    real zr = -d, zi = (real)1.0 / rdt, den = zr * zr + zi * zi;
+                    c.M[i].re = zr / den; c.M[i].im = -zi / den;
+                }
+            }
+            lap_rot(&g, psim, c.cD, c.Om, c.dd, c.rr, c.lap);
+            for (int64_t i = 0; i < N; i++) {
+                real vv = Vr ? Vr[i] : 0, a2 = psim[i].re * psim[i].re + psim[i].im * psim[i].im;
+                real f = vv + rbeta * a2;
+                real dr = phi1[i].re - p[i].re, di = phi1[i].im - p[i].im;
+                if (!tsch) {
+                    c.b[i].re = (c.idt * dr + f * psim[i].re) - c.lap[i].re;
+                    c.b[i].im = (c.idt * di + f * psim[i].im) - c.lap[i].im;
+                } else {   /* (i/dt)(phi1 - phi) - f psi + lapRot(psi) */
+                    c.b[i].re = (-(c.idt * di) - f * psim[i].re) + c.lap[i].re;
+                    c.b[i].im = ((c.idt * dr) - f * psim[i].im) + c.lap[i].im;
+                }
+            }
+            ktot += krylov_solve(&c, phiw, nkrylov, (real)tolkrylov, 1, w, tmp);
+            for (int64_t i = 0; i < N; i++) { phi1[i].re -= phiw[i].re; phi1[i].im -= phiw[i].im; }
+            for (int64_t i = 0; i < N; i++) tmp[i] = phiw[i].re * phiw[i].re + phiw[i].im * phiw[i].im;
+            if (RSQRT(pairwise_sum(tmp, N)) < (real)tolnewton) break;
+        }
+        for (int64_t i = 0; i < N; i++) p[i] = phi1[i];
+        if (!tsch) {
+            real nrm = field_norm(&g, p);
+            for (int64_t i = 0; i < N; i++) { p[i].re /= nrm; p[i].im /= nrm; }
+        }
+    }
+    if (rc == 0) store_field(p, psi, N);
+    if (kry_total) *kry_total = ktot;
+    for (size_t i = 0; i < sizeof(allc) / sizeof(allc[0]); i++) free(*allc[i]);
+    free(c.Anl); free(tmp); free(p); free(Vr);
     grid_free(&g);
     return rc;
 }

@@ -66,6 +66,11 @@ class _Bound:
         self.or_rk_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        self.or_implicit_step = g("or_implicit_step")
+        self.or_implicit_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_double, _i64p]
         self.or_max_threads = g("or_max_threads")
         self.or_max_threads.restype = ctypes.c_int
 
@@ -242,6 +247,139 @@ def np_rk_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=
         if filter == "solution":
             p = filt(p)
     return np.asfortranarray(p)
+
+
+IMPLICIT_SCHEMES = {"BackwardEuler": 0, "BackwardEulerNoPrecond": 1, "CrankNicolson": 2,
+                    "CrankNicolsonQuasiNewton": 3, "CrankNicolsonT": 4, "CrankNicolsonQuasiNewtonT": 5}
+
+
+def c_implicit_step(psi, bounds, *, scheme="BackwardEuler", coeffD=-0.5, beta=1.0, omega=0.0, V=None,
+                    nsteps=1, dt=1e-3, nkrylov=70, tolkrylov=1e-8, nnewton=15, tolnewton=1e-6,
+                    extended=False):
+    """nsteps of one implicit scheme (backward-euler.jl / crank-nicolson.jl with
+    the BiCGStab of krylov.jl).  Returns (psi, total Krylov count)."""
+    out = _field(psi).copy(order="F")
+    nd, n, lo, hi = _geom(out.shape, bounds)
+    Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
+    tot = np.zeros(1, dtype=np.int64)
+    rc = lib(extended).or_implicit_step(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega,
+                                        _p(Vp), _p(out), int(nsteps), IMPLICIT_SCHEMES[scheme], float(dt),
+                                        int(nkrylov), float(tolkrylov), int(nnewton), float(tolnewton),
+                                        tot.ctypes.data_as(_i64p))
+    if rc != 0:
+        raise ValueError("or_implicit_step failed")
+    return out, int(tot[0])
+
+
+def np_implicit_step(psi, bounds, *, scheme="BackwardEuler", coeffD=-0.5, beta=1.0, omega=0.0, V=None,
+                     nsteps=1, dt=1e-3, nkrylov=70, tolkrylov=1e-8, nnewton=15, tolnewton=1e-6):
+    """The same schemes with numpy.fft and numpy reductions (independent of the
+    C restatement): lapRot as the sum of the per-axis spectral multipliers."""
+    p = np.array(psi, dtype=np.complex128, order="F", copy=True)
+    nd = p.ndim
+    d = spacing(p.shape, bounds)
+    xs = [grid_coords(n, b[0], b[1]) for n, b in zip(p.shape, bounds)]
+    xis = [fftfreq(n, dd) for n, dd in zip(p.shape, d)]
+    Vv = 0.0 if V is None else np.asarray(V, dtype=np.float64)
+
+    def bshape(v, axis):
+        sh = [1] * nd
+        sh[axis] = v.size
+        return v.reshape(sh)
+
+    def lap_rot(q):
+        out = np.zeros_like(q)
+        for a in range(nd):
+            xi = bshape(xis[a], a)
+            if a == 0 and nd >= 2:
+                m = coeffD * (xi * xi) - omega * bshape(xs[1], 1) * xi
+            elif a == 1:
+                m = coeffD * (xi * xi) + omega * bshape(xs[0], 0) * xi
+            else:
+                m = coeffD * (xi * xi)
+            out += np.fft.ifft(m * np.fft.fft(q, axis=a), axis=a)
+        return out
+
+    idt = 1.0 / dt
+    st = {}
+
+    def prodA(x):
+        L = lap_rot(x)
+        if scheme == "BackwardEuler":
+            return x - st["M"] * L
+        if scheme == "BackwardEulerNoPrecond":
+            return (idt + st["Anl"]) * x - L
+        if scheme == "CrankNicolson":
+            return (idt + st["Anl"]) * x + 0.5 * st["Anl2"] * np.conj(x) - 0.5 * L
+        if scheme == "CrankNicolsonQuasiNewton":
+            return (idt + st["Anl"] * 0.5) * x - 0.5 * L
+        if scheme == "CrankNicolsonT":
+            return (1j * idt - 0.5 * st["Anl"]) * x - 0.5 * st["Anl2"] * np.conj(x) + 0.5 * L
+        return (1j * idt - st["Anl"] * 0.5) * x + 0.5 * L
+
+    def rdot(a, b):
+        return float(np.sum((a * np.conj(b)).real))
+
+    def krylov(phi, precond):
+        M = st["M"] if precond else 1.0
+        b = st["b"]
+        normb = np.sqrt(rdot(M * b, M * b))
+        r = M * (b - prodA(phi))
+        r2 = r.copy()
+        pp = r.copy()
+        niter = 0
+        for it in range(1, nkrylov + 1):
+            Ap = M * prodA(pp)
+            rr2 = rdot(r, r2)
+            alpha = rr2 / rdot(Ap, r2)
+            s_ = r - alpha * Ap
+            As = M * prodA(s_)
+            omega_ = rdot(As, s_) / rdot(As, As)
+            phi += alpha * pp + omega_ * s_
+            rr2old = rdot(r, r2)
+            r = s_ - omega_ * As
+            if np.sqrt(rdot(r, r)) / normb < tolkrylov:
+                break
+            niter = it
+            beta_ = rdot(r, r2) / rr2old * alpha / omega_
+            pp = r + beta_ * (pp - omega_ * Ap)
+        return niter
+
+    def normalize(q):
+        return q / (np.sqrt(np.sum(np.abs(q) ** 2)) * np.sqrt(np.prod(d)))
+
+    tot = 0
+    for _ in range(nsteps):
+        if scheme in ("BackwardEuler", "BackwardEulerNoPrecond"):
+            a2 = np.abs(p) ** 2
+            st["M"] = 1.0 / (idt + Vv + beta * a2)
+            st["Anl"] = Vv + beta * a2
+            st["b"] = st["M"] * p / dt if scheme == "BackwardEuler" else p / dt
+            tot += krylov(p, False)
+            p = normalize(p)
+            continue
+        tsch = scheme.endswith("T")
+        newton = scheme in ("CrankNicolson", "CrankNicolsonT")
+        phi1 = p.copy()
+        phiw = np.zeros_like(p)
+        for _ in range(nnewton):
+            q = 0.5 * (phi1 + p)
+            a2 = np.abs(q) ** 2
+            st["Anl"] = Vv + (2 if newton else 3) * beta * a2
+            st["Anl2"] = beta * q * q
+            dd = (Vv + 3 * beta * a2) * 0.5
+            st["M"] = 1.0 / ((1j * idt - dd) if tsch else (idt + dd))
+            f = Vv + beta * a2
+            if tsch:
+                st["b"] = 1j * idt * (phi1 - p) - f * q + lap_rot(q)
+            else:
+                st["b"] = idt * (phi1 - p) + f * q - lap_rot(q)
+            tot += krylov(phiw, True)
+            phi1 = phi1 - phiw
+            if np.sqrt(np.sum(np.abs(phiw) ** 2)) < tolnewton:
+                break
+        p = phi1 if tsch else normalize(phi1)
+    return np.asfortranarray(p), tot
 
 
 def c_derivatives(psi, bounds):

@@ -38,7 +38,9 @@ from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_NOMASSLOCK, GPSS_F
 
 __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "PotentialZero",
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
-           "solve", "BatchSplit2", "GPSSError", "version", "NumModelGPRK"]
+           "solve", "BatchSplit2", "GPSSError", "version", "NumModelGPRK", "NumModelBackwardEuler", "NumModelBackwardEulerNoPrecond",
+           "NumModelCrankNicolson", "NumModelCrankNicolsonQuasiNewton", "NumModelCrankNicolsonT",
+           "NumModelCrankNicolsonQuasiNewtonT"]
 
 _f64p = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -336,6 +338,9 @@ class _SplitModel:
                                          ctypes.byref(loss), dv.ctypes.data_as(_f64p), gp.ctypes.data_as(_f64p)))
         return loss.value, dv, gp
 
+    def timestep_value(self):
+        return self.scheme
+
     @property
     def handle(self):
         return self._h
@@ -394,11 +399,93 @@ class NumModelGPRK(_SplitModel):
                 f"  └──────────── solve: number of iterations {self.niter}, backup frequency {self.freqbckp}")
 
 
+class _ImplicitModel(_SplitModel):
+    """Common part of the implicit schemes: a linear system per step (per
+    Newton iteration for Crank-Nicolson) solved by the reference's BiCGStab
+    (krylov.jl).  timeStep returns the summed Krylov counts, as the reference's
+    timeStep! does."""
+    scheme = 0
+    implicit = 0
+    newton = False
+
+    def __init__(self, f: Field, param: GrossPitaevskiiParameters, dt, niter, freqbckp, *, nkrylov=70,
+                 tolkrylov=1e-8, nnewton=15, tolnewton=1e-6, precision="fp64", writers=()):
+        self.nkrylov = int(nkrylov)
+        self.tolkrylov = float(tolkrylov)
+        self.nnewton = int(nnewton)
+        self.tolnewton = float(tolnewton)
+        self.last_krylov = 0
+        super().__init__(f, param, dt, niter, freqbckp, precision=precision, writers=writers)
+
+    def step(self, nsteps=1, imag=False, diag=False):
+        k = ctypes.c_int64()
+        self._ck(_lib.lib().gpss_implicit_step(self._h, int(nsteps), self.implicit, self.dt, self.nkrylov,
+                                               self.tolkrylov, self.nnewton, self.tolnewton, ctypes.byref(k)))
+        self._device_newer = True
+        self.last_krylov = k.value
+        if diag:
+            eom, edel, ebeta, e, mu = self.energies()
+            return {"mass": self.mass(), "energy": (eom, edel, ebeta, e, mu), "steps": int(nsteps)}
+        return None
+
+    def timestep_value(self):
+        return self.last_krylov
+
+    def __repr__(self):
+        lines = [self._title, f"  ├──────────  krylov: n iterations {self.nkrylov}, tolerance {self.tolkrylov}"]
+        if self.newton:
+            lines.append(f"  ├──────────  newton: n iterations {self.nnewton}, tolerance {self.tolnewton}")
+        lines += [f"  ├───────  time step: {self.dt}",
+                  f"  └──────────── solve: number of iterations {self.niter}, backup frequency {self.freqbckp}"]
+        return "\n".join(lines)
+
+
+class NumModelBackwardEuler(_ImplicitModel):
+    """Preconditioned backward Euler in imaginary time (backward-euler.jl:1-90)."""
+    implicit = 0
+    _title = "Backward Euler"
+
+
+class NumModelBackwardEulerNoPrecond(_ImplicitModel):
+    """Backward Euler without preconditioning (backward-euler.jl:92-197)."""
+    implicit = 1
+    _title = "Backward Euler without preconditionning"
+
+
+class NumModelCrankNicolson(_ImplicitModel):
+    """Stationary Crank-Nicolson, Newton-Raphson (crank-nicolson.jl:1-123)."""
+    implicit = 2
+    newton = True
+    _title = "Stationnary Crank-Nicolson Newton-Raphson scheme"
+
+
+class NumModelCrankNicolsonQuasiNewton(_ImplicitModel):
+    """Stationary Crank-Nicolson, quasi-Newton (crank-nicolson.jl:125-245)."""
+    implicit = 3
+    newton = True
+    _title = "Stationnary Crank-Nicolson Quasi-Newton scheme"
+
+
+class NumModelCrankNicolsonT(_ImplicitModel):
+    """Time-dependent Crank-Nicolson, Newton-Raphson (crank-nicolson.jl:247-368)."""
+    implicit = 4
+    newton = True
+    _title = "Time dependant Crank-Nicolson Newton-Raphson scheme"
+
+
+class NumModelCrankNicolsonQuasiNewtonT(_ImplicitModel):
+    """Time-dependent Crank-Nicolson, quasi-Newton (crank-nicolson.jl:370-489)."""
+    implicit = 5
+    newton = True
+    _title = "Time dependant Crank-Nicolson Quasi-Newton scheme"
+
+
 def timeStep(n: _SplitModel, nsteps: int = 1) -> int:
-    """timeStep!(n): one (or nsteps) split steps; returns the reference's
-    per-step count (1 for Lie, 2 for Strang; splitting.jl:81, 153)."""
+    """timeStep!(n): one (or nsteps) steps; returns what the reference's
+    timeStep! returns (1 for Lie, 2 for Strang, splitting.jl:81, 153; 0 for
+    explicit RK; the Krylov iteration count for the implicit schemes)."""
     n.step(nsteps)
-    return n.scheme
+    return n.timestep_value()
 
 
 def energy(n: _SplitModel, show: bool = False):

@@ -64,6 +64,9 @@ SIGNATURES = {
     "gpss_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                  ctypes.POINTER(Diag)]),
     "gpss_rk_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    "gpss_implicit_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                          ctypes.POINTER(ctypes.c_int64)]),
     "gpss_energy": (ctypes.c_int, [_vp, _f64p]),
     "gpss_mass": (ctypes.c_int, [_vp, _f64p]),
     "gpss_norm": (ctypes.c_int, [_vp, _f64p]),

@@ -51,6 +51,8 @@ struct gpss_ctx {
     std::vector<PhaseEntry> phases;
     void *rk_buf[4] = {nullptr, nullptr, nullptr, nullptr};  // RK: stage state, lapRot, NL term, sum
     int *rk_lim = nullptr;    // RK: 2/3-rule limits per inner position (launch_mask_spectrum)
+    void *im_buf = nullptr;   // implicit schemes: work fields (implicit_impl)
+    size_t im_bytes = 0;
     // discrete adjoint: buffers kept between calls (sized for adj_nck checkpoints, adj_K states)
     void *adj_buf = nullptr;
     size_t adj_bytes = 0;
@@ -970,20 +972,28 @@ template <typename T> static int dealias_field(gpss_ctx *c, void *f)
     return transform_all<T>(c, f, true);
 }
 
+// out = lapRot(q) (GrossPitaevskii.jl:12-45) as one fused pass per axis with
+// the axis multiplier table, the y/z passes adding into the x result
+template <typename T> static int lap_rot_dev(gpss_ctx *c, const void *q, void *out)
+{
+    for (int axis = 0; axis < c->ndim; axis++) {
+        PassArgs<T> a = axis_args<T>(c, axis, q, out);
+        const void *ph;
+        GPSS_TRY(get_phase(c, axis, 0.0, 2, 1, &ph, &a.prow));
+        a.phase = (const vec2<T> *)ph;
+        if (axis > 0) a.acc = (const vec2<T> *)out;
+        GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
+    }
+    return GPSS_OK;
+}
+
 // k = i (lapRot(q) - N(q)) folded into the stage update (launch_rk_combine)
 template <typename T>
 static int rk_stage(gpss_ctx *c, const void *q, int filter, int acc_mode, double acc_w, double cf, int from_acc,
                     void *out)
 {
     void *k = c->rk_buf[1], *t = c->rk_buf[2], *acc = c->rk_buf[3];
-    for (int axis = 0; axis < c->ndim; axis++) {
-        PassArgs<T> a = axis_args<T>(c, axis, q, k);
-        const void *ph;
-        GPSS_TRY(get_phase(c, axis, 0.0, 2, 1, &ph, &a.prow));
-        a.phase = (const vec2<T> *)ph;
-        if (axis > 0) a.acc = (const vec2<T> *)k;
-        GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
-    }
+    GPSS_TRY(lap_rot_dev<T>(c, q, k));
     cudaError_t e = launch_nl_term<T>((const vec2<T> *)q, c->have_V ? (const T *)c->V : nullptr, c->beta,
                                       (vec2<T> *)t, c->total, c->stream);
     if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl_term: %s", cudaGetErrorString(e));
@@ -1033,6 +1043,170 @@ template <typename T> static int rk_step_impl(gpss_ctx *c, int nsteps, int stepp
     return GPSS_OK;
 }
 
+// ------------------------------------------- implicit schemes (BE / CN) ----
+// timeStep! of NumModelBackwardEuler[NoPrecond] (backward-euler.jl:62-83,
+// 155-172) and NumModelCrankNicolson[QuasiNewton][T] (crank-nicolson.jl:62-103,
+// 186-225, 308-347, 432-468) with the BiCGStab of krylov.jl.  lapRot is the
+// fused multiplier passes; the operators, right-hand sides and vector updates
+// are the pointwise kernels of implicit.cu; each Krylov iteration reads back
+// its dot products (the scalars and the stopping test are the reference's).
+
+struct ImBufs {
+    void *r, *r2, *p, *Ap, *s, *As, *lap, *b, *M, *Anl2, *psim, *phi1, *phiw, *Anl;
+    double *partials, *dots;
+};
+
+template <typename T> static int im_bufs(gpss_ctx *c, ImBufs &B)
+{
+    const size_t fb = (size_t)c->total * sizeof(vec2<T>);
+    const size_t rb = (size_t)c->total * sizeof(T);
+    const size_t pb = sizeof(double) * (2 * 152 * 8 + 2);
+    const size_t need = 13 * fb + rb + pb;
+    if (!c->im_buf || c->im_bytes < need) {
+        if (c->im_buf) { cudaStreamSynchronize(c->stream); cudaFree(c->im_buf); c->im_buf = nullptr; }
+        GPSS_TRY(dev_alloc(c, &c->im_buf, need));
+        c->im_bytes = need;
+    }
+    char *base = static_cast<char *>(c->im_buf);
+    void **f[13] = {&B.r, &B.r2, &B.p, &B.Ap, &B.s, &B.As, &B.lap, &B.b, &B.M, &B.Anl2, &B.psim, &B.phi1, &B.phiw};
+    for (int i = 0; i < 13; i++) *f[i] = base + (size_t)i * fb;
+    B.Anl = base + 13 * fb;
+    B.partials = reinterpret_cast<double *>(base + 13 * fb + rb);
+    B.dots = B.partials + 2 * 152 * 8;
+    return GPSS_OK;
+}
+
+#define IM_TRY(call)                                                                   \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) return fail(c, GPSS_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+        c->launches++;                                                                 \
+    } while (0)
+
+// two dot products Sum Re(a conj b) (FP64) read back to the host
+template <typename T>
+static int im_dots(gpss_ctx *c, ImBufs &B, const void *a1, const void *b1, const void *a2, const void *b2,
+                   double out[2])
+{
+    using V = vec2<T>;
+    IM_TRY(im_dot2<T>((const V *)a1, (const V *)b1, (const V *)a2, (const V *)b2, c->total, B.partials, B.dots,
+                      c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(out, B.dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GPSS_OK;
+}
+
+// out = [M] prodA(x) or [M](b - prodA(x))
+template <typename T>
+static int im_apply(gpss_ctx *c, ImBufs &B, int scheme, double dt, const void *x, bool bsub, int precond, void *out)
+{
+    using V = vec2<T>;
+    GPSS_TRY(lap_rot_dev<T>(c, x, B.lap));
+    IM_TRY(im_op<T>((const V *)x, (const V *)B.lap, scheme, dt, (const V *)B.M, (const T *)B.Anl,
+                    (const V *)B.Anl2, bsub ? (const V *)B.b : nullptr, precond, (V *)out, c->total, c->stream));
+    return GPSS_OK;
+}
+
+// krylov! (precond = 0) / krylovPreCond! (precond = 1), krylov.jl:1-67
+template <typename T>
+static int im_krylov(gpss_ctx *c, ImBufs &B, int scheme, double dt, void *phi, int nkrylov, double tol, int precond,
+                     int *niter_out)
+{
+    using V = vec2<T>;
+    const size_t fb = (size_t)c->total * sizeof(V);
+    double d[2];
+    if (precond) {
+        IM_TRY(im_mfield<T>((V *)B.s, (const V *)B.M, (const V *)B.b, c->total, c->stream));
+        GPSS_TRY(im_dots<T>(c, B, B.s, B.s, nullptr, nullptr, d));
+    } else {
+        GPSS_TRY(im_dots<T>(c, B, B.b, B.b, nullptr, nullptr, d));
+    }
+    const double normb = std::sqrt(d[0]);
+    GPSS_TRY(im_apply<T>(c, B, scheme, dt, phi, true, precond, B.r));
+    CUDA_TRY(c, cudaMemcpyAsync(B.r2, B.r, fb, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(B.p, B.r, fb, cudaMemcpyDeviceToDevice, c->stream));
+    int niter = 0;
+    for (int it = 1; it <= nkrylov; it++) {
+        GPSS_TRY(im_apply<T>(c, B, scheme, dt, B.p, false, precond, B.Ap));
+        GPSS_TRY(im_dots<T>(c, B, B.r, B.r2, B.Ap, B.r2, d));
+        const double rr2 = d[0], alpha = d[0] / d[1];
+        IM_TRY(im_axmy<T>((V *)B.s, (const V *)B.r, alpha, (const V *)B.Ap, c->total, c->stream));
+        GPSS_TRY(im_apply<T>(c, B, scheme, dt, B.s, false, precond, B.As));
+        GPSS_TRY(im_dots<T>(c, B, B.As, B.s, B.As, B.As, d));
+        const double omega = d[0] / d[1];
+        IM_TRY(im_update<T>((V *)phi, (const V *)B.p, (const V *)B.s, (const V *)B.As, (V *)B.r, alpha, omega,
+                            c->total, c->stream));
+        GPSS_TRY(im_dots<T>(c, B, B.r, B.r, B.r, B.r2, d));
+        if (!std::isfinite(d[0])) return fail(c, GPSS_ENONFINITE, "Krylov solver: non-finite residual");
+        if (std::sqrt(d[0]) / normb < tol) break;
+        niter = it;
+        const double beta = d[1] / rr2 * alpha / omega;
+        IM_TRY(im_pdir<T>((V *)B.p, (const V *)B.r, (const V *)B.Ap, beta, omega, c->total, c->stream));
+    }
+    *niter_out = niter;
+    return GPSS_OK;
+}
+
+template <typename T> static int normalize_impl(gpss_ctx *c);
+
+template <typename T>
+static int implicit_impl(gpss_ctx *c, int nsteps, int scheme, double dt, int nkrylov, double tol, int nnewton,
+                         double tolnewton, int64_t *ktot)
+{
+    using V = vec2<T>;
+    ImBufs B;
+    GPSS_TRY(im_bufs<T>(c, B));
+    const size_t fb = (size_t)c->total * sizeof(V);
+    const T *Vp = c->have_V ? (const T *)c->V : nullptr;
+    int64_t total_k = 0;
+    for (int st = 0; st < nsteps; st++) {
+        int nk = 0;
+        if (scheme == IM_SCHEME_BE || scheme == IM_SCHEME_BE_NOPRE) {
+            IM_TRY(im_prep_be<T>((const V *)c->psi, Vp, c->beta, dt, scheme, (V *)B.M, (T *)B.Anl, (V *)B.b,
+                                 c->total, c->stream));
+            GPSS_TRY(im_krylov<T>(c, B, scheme, dt, c->psi, nkrylov, tol, 0, &nk));
+            total_k += nk;
+            GPSS_TRY(normalize_impl<T>(c));
+            continue;
+        }
+        const int tsch = scheme == IM_SCHEME_CN_T || scheme == IM_SCHEME_CN_QN_T;
+        CUDA_TRY(c, cudaMemcpyAsync(B.phi1, c->psi, fb, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(c, cudaMemsetAsync(B.phiw, 0, fb, c->stream));
+        for (int itn = 1; itn <= nnewton; itn++) {
+            IM_TRY(im_prep_cn<T>((const V *)c->psi, (const V *)B.phi1, Vp, c->beta, dt, scheme, (V *)B.psim,
+                                 (T *)B.Anl, (V *)B.Anl2, (V *)B.M, c->total, c->stream));
+            GPSS_TRY(lap_rot_dev<T>(c, B.psim, B.lap));
+            IM_TRY(im_rhs_cn<T>((const V *)c->psi, (const V *)B.phi1, (const V *)B.psim, (const V *)B.lap, Vp,
+                                c->beta, dt, tsch, (V *)B.b, c->total, c->stream));
+            GPSS_TRY(im_krylov<T>(c, B, scheme, dt, B.phiw, nkrylov, tol, 1, &nk));
+            total_k += nk;
+            IM_TRY(im_axmy<T>((V *)B.phi1, (const V *)B.phi1, 1.0, (const V *)B.phiw, c->total, c->stream));
+            double d[2];
+            GPSS_TRY(im_dots<T>(c, B, B.phiw, B.phiw, nullptr, nullptr, d));
+            if (std::sqrt(d[0]) < tolnewton) break;
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(c->psi, B.phi1, fb, cudaMemcpyDeviceToDevice, c->stream));
+        if (!tsch) GPSS_TRY(normalize_impl<T>(c));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (ktot) *ktot = total_k;
+    return GPSS_OK;
+}
+
+// normalize! (Fields.jl:196-200) on the device: unit mass from the FP64 sum
+template <typename T> static int normalize_impl(gpss_ctx *c)
+{
+    int zero = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GPSS_TRY(diag_passes<T>(c, false, FIN_UNITMASS));
+    GPSS_TRY(apply_scale<T>(c));
+    int st = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (st) return fail(c, GPSS_ENONFINITE, "normalize: non-finite or zero norm");
+    return GPSS_OK;
+}
+
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
 extern "C" {
@@ -1054,7 +1228,7 @@ void gpss_destroy(gpss_ctx *c)
     void *ptrs[] = {c->psi, c->scratch, c->V, c->tw[0], c->tw[1], c->tw[2], c->coord_dev[0],
                     c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status,
                     c->counter, c->rk_buf[0], c->rk_buf[1], c->rk_buf[2], c->rk_buf[3], c->rk_lim,
-                    c->adj_buf};
+                    c->adj_buf, c->im_buf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : c->ev)
@@ -1246,6 +1420,23 @@ int gpss_rk_step(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
                                      : rk_step_impl<double>(c, nsteps, stepper, filter, dt);
 }
 
+int gpss_implicit_step(gpss_ctx *c, int nsteps, int scheme, double dt, int nkrylov, double tolkrylov, int nnewton,
+                       double tolnewton, int64_t *krylov_iters)
+{
+    if (!c) return GPSS_EINVAL;
+    if (!c->have_psi) return fail(c, GPSS_ESTATE, "gpss_implicit_step: no field uploaded");
+    if (nsteps < 0 || nkrylov < 1 || nnewton < 1)
+        return fail(c, GPSS_EINVAL, "gpss_implicit_step: need nsteps >= 0, nkrylov >= 1, nnewton >= 1");
+    if (scheme < GPSS_IMPLICIT_BE || scheme > GPSS_IMPLICIT_CN_QN_T)
+        return fail(c, GPSS_EINVAL, "gpss_implicit_step: unknown scheme %d", scheme);
+    if (!(dt > 0.0) || !std::isfinite(dt) || !(tolkrylov > 0.0) || !(tolnewton > 0.0))
+        return fail(c, GPSS_EINVAL, "gpss_implicit_step: dt and the tolerances must be positive");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    return c->precision == GPSS_FP32
+               ? implicit_impl<float>(c, nsteps, scheme, dt, nkrylov, tolkrylov, nnewton, tolnewton, krylov_iters)
+               : implicit_impl<double>(c, nsteps, scheme, dt, nkrylov, tolkrylov, nnewton, tolnewton, krylov_iters);
+}
+
 int gpss_energy(gpss_ctx *c, double *out)
 {
     if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_energy: null out") : GPSS_EINVAL;
@@ -1295,18 +1486,7 @@ int gpss_normalize(gpss_ctx *c)
     if (!c) return GPSS_EINVAL;
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    int zero = 0;
-    CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, FIN_UNITMASS)
-                                       : diag_passes<double>(c, false, FIN_UNITMASS);
-    if (rc) return rc;
-    rc = c->precision == GPSS_FP32 ? apply_scale<float>(c) : apply_scale<double>(c);
-    if (rc) return rc;
-    int st = 0;
-    CUDA_TRY(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    if (st) return fail(c, GPSS_ENONFINITE, "normalize: non-finite or zero norm");
-    return GPSS_OK;
+    return c->precision == GPSS_FP32 ? normalize_impl<float>(c) : normalize_impl<double>(c);
 }
 
 int gpss_ground_state(gpss_ctx *c, double dt, double tol, int64_t max_steps, int check_every,

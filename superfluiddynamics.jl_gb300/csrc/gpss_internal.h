@@ -50,6 +50,37 @@ cudaError_t launch_nl(vec2<T> *psi, const T *V, double beta, double dt, int imag
                       cudaStream_t s);
 template <typename T>
 cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s);
+// implicit schemes (implicit.cu); the scheme numbers are the GPSS_IMPLICIT_* of gpss.h
+enum {
+    IM_SCHEME_BE = 0, IM_SCHEME_BE_NOPRE = 1, IM_SCHEME_CN = 2, IM_SCHEME_CN_QN = 3, IM_SCHEME_CN_T = 4,
+    IM_SCHEME_CN_QN_T = 5
+};
+template <typename T>
+cudaError_t im_prep_be(const vec2<T> *phi, const T *V, double beta, double dt, int scheme, vec2<T> *M, T *Anl,
+                       vec2<T> *b, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_prep_cn(const vec2<T> *phi, const vec2<T> *phi1, const T *V, double beta, double dt, int scheme,
+                       vec2<T> *psim, T *Anl, vec2<T> *Anl2, vec2<T> *M, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_rhs_cn(const vec2<T> *phi, const vec2<T> *phi1, const vec2<T> *psim, const vec2<T> *lap, const T *V,
+                      double beta, double dt, int tsch, vec2<T> *b, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_op(const vec2<T> *x, const vec2<T> *lap, int scheme, double dt, const vec2<T> *M, const T *Anl,
+                  const vec2<T> *Anl2, const vec2<T> *b, int precond, vec2<T> *out, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_dot2(const vec2<T> *a1, const vec2<T> *b1, const vec2<T> *a2, const vec2<T> *b2, int64_t total,
+                    double *partials, double *out, cudaStream_t s);
+template <typename T>
+cudaError_t im_axmy(vec2<T> *out, const vec2<T> *x, double alpha, const vec2<T> *y, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_update(vec2<T> *phi, const vec2<T> *p, const vec2<T> *sv, const vec2<T> *As, vec2<T> *r, double alpha,
+                      double omega, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_pdir(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, double beta, double omega, int64_t total,
+                    cudaStream_t s);
+template <typename T>
+cudaError_t im_mfield(vec2<T> *out, const vec2<T> *M, const vec2<T> *x, int64_t total, cudaStream_t s);
+
 // explicit Runge-Kutta helpers (pointwise.cu)
 template <typename T>
 cudaError_t launch_nl_term(const vec2<T> *q, const T *V, double beta, vec2<T> *t, int64_t total, cudaStream_t s);

@@ -61,6 +61,7 @@ def test_null_arguments(L):
     assert L.gpss_set_params(None, 0, 0, 0) == -1
     assert L.gpss_step(None, 1, 2, 0, 1e-3, None) == -1
     assert L.gpss_rk_step(None, 1, 4, 1, 1e-3) == -1
+    assert L.gpss_implicit_step(None, 1, 0, 1e-3, 70, 1e-8, 15, 1e-6, None) == -1
     L.gpss_destroy(None)
 
 
