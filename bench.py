@@ -5,7 +5,8 @@ Workload (cfg1): 3D real-time GP, Strang splitting (NumModelSplit2), 256^3
 periodic box [0, 2pi]^3, V = 0, coeffD = -xi/sqrt(2), beta = 1/(sqrt(2) xi),
 xi = 0.05, psi0 = e^{i theta} with 64 seeded Fourier modes; dt = 2.5e-3.
 One bench step = one cfg1 run of 200 time steps through gpss_step (FP32 fused
-kernels, FP64 reductions), on a field resident in HBM.
+kernels, FP64 reductions) from the cfg1 initial field, which is restored in
+HBM (outside the timed events) before every bench step.
 
 Metric: Mcell-steps/s = cells x time steps / seconds.  The field (134 MB FP32)
 is larger than L2 and every pass streams 268 MB, so no L2 flush is needed.
@@ -407,26 +408,42 @@ def run_gpss(args, rank, world, local):
     h = model.handle
     ck = lambda rc: _lib.check(rc, h)
 
-    # ---- device-resident throughput (value)
+    # ---- device-resident throughput (value).  Every bench step is the cfg1
+    # run itself: the initial field is restored (uploaded, outside the timed
+    # events) before each one, so the run never drifts into a different state
+    # (the nonlinear epilogue's cost depends on the field through |psi|^2).
+    psi0 = np.asfortranarray(c["psi"], dtype=np.complex128)
+    p0 = psi0.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    def restore():
+        ck(L.gpss_upload(h, p0))
+        ck(L.gpss_sync(h))
+
     for _ in range(args.warmup):
+        restore()
         ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
     ck(L.gpss_sync(h))
     dist.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    l0 = L.gpss_launch_count(h)
-    ck(L.gpss_event_record(h, 0))
-    for _ in range(args.steps):
-        ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
-    ck(L.gpss_event_record(h, 1))
+    launches = 0
+    t_sum = 0.0
     ms = ctypes.c_float()
-    ck(L.gpss_event_elapsed(h, 0, 1, ctypes.byref(ms)))
-    launches = L.gpss_launch_count(h) - l0
+    for _ in range(args.steps):
+        restore()
+        l0 = L.gpss_launch_count(h)
+        ck(L.gpss_event_record(h, 0))
+        ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+        ck(L.gpss_event_record(h, 1))
+        ck(L.gpss_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+        launches += L.gpss_launch_count(h) - l0
+        t_sum += ms.value
     clk = clocks.stop()
     dist.barrier()
-    t_ms = dist.max(ms.value)
+    t_ms = dist.max(t_sum)
     value = world * cells * nt * args.steps / (t_ms / 1e3) / 1e6
+    restore()
 
     # ---- dominant kernel timing (roofline): each fused pass alone, CUDA events
     per_axis = {}
@@ -534,6 +551,7 @@ def run_gpss(args, rank, world, local):
                                "V=0, xi=0.05, c=1, dt=2.5e-3, FP32 fused kernels",
                    "grid": [args.n] * 3, "timesteps_per_step": nt,
                    "l2": "inputs larger than L2 (134 MB field, 268 MB streamed per pass); no flush",
+                   "initial_field": "restored before every bench step (outside the timed events)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gpu_launches": int(launches),
         "e2e": None if e2e is None else {"value": e2e, "unit": "Mcell-steps/s", "h2d_bytes_per_step": nbytes,
