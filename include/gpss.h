@@ -202,8 +202,14 @@ int gpss_batch_set_run(gpss_batch *b, int run, double beta, const double *V, con
 int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out);
 int gpss_batch_download(gpss_batch *b, int run, double *psi);
 /* the autotuner's choice (policy 0: runs up to 128^2 in shared memory; 1: up to 64^2),
- * queue order (0: largest first, 1: as given) and the four trial times in ms */
-int gpss_batch_tuning(const gpss_batch *b, int *policy, int *order, float *trial_ms);
+ * queue order (0: largest first, 1: as given), stacking (1: the 256^2 runs of a box go
+ * through the directional pass kernels as one stack of planes) and the trial times in ms
+ * (8 entries: index = 4 stack + 2 policy + order; stacked trials only when a box holds
+ * two or more 256^2 runs) */
+int gpss_batch_tuning(const gpss_batch *b, int *policy, int *order, int *stack, float *trial_ms);
+/* fix the launch choice instead of autotuning it (stack = 1 needs a box holding two
+ * or more 256^2 runs; otherwise it is ignored) */
+int gpss_batch_set_tuning(gpss_batch *b, int policy, int order, int stack);
 
 /* ---- timing and integration helpers (no reference counterpart) ---- */
 

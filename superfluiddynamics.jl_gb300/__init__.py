@@ -577,10 +577,15 @@ class BatchSplit2:
         return out
 
     def tuning(self):
-        pol, order = ctypes.c_int(), ctypes.c_int()
-        ms = (ctypes.c_float * 4)()
-        self._ck(_lib.lib().gpss_batch_tuning(self._h, ctypes.byref(pol), ctypes.byref(order), ms))
-        return {"policy": pol.value, "order": order.value, "trial_ms": list(ms)}
+        pol, order, stack = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_float * 8)()
+        self._ck(_lib.lib().gpss_batch_tuning(self._h, ctypes.byref(pol), ctypes.byref(order), ctypes.byref(stack),
+                                              ms))
+        return {"policy": pol.value, "order": order.value, "stack": stack.value, "trial_ms": list(ms)}
+
+    def set_tuning(self, policy, order, stack=0):
+        """Fix the launch choice (skips the autotuner)."""
+        self._ck(_lib.lib().gpss_batch_set_tuning(self._h, int(policy), int(order), int(stack)))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -81,8 +81,9 @@ SIGNATURES = {
     "gpss_batch_set_run": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _f64p, _f64p]),
     "gpss_batch_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _f64p]),
     "gpss_batch_download": (ctypes.c_int, [_vp, ctypes.c_int, _f64p]),
+    "gpss_batch_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "gpss_batch_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
-                                         ctypes.POINTER(ctypes.c_float)]),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]),
     "gpss_sync": (ctypes.c_int, [_vp]),
     "gpss_event_record": (ctypes.c_int, [_vp, ctypes.c_int]),
     "gpss_event_elapsed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,

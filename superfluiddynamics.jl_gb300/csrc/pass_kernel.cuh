@@ -71,7 +71,30 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //   FEAT_NL    nonlinear epilogue and the mass sum
 //   FEAT_DIAG  energy sums (RED_POINT, RED_KIN), rotation (per-row phases),
 //              accumulation into a second field
-enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3 };
+//   FEAT_PLANE a stack of independent 2D runs of one shape (planes): the
+//              nonlinear constants and the deferred renormalisation factor
+//              are per plane (plane_nl, plane_scale)
+enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4 };
+
+// A renormalisation factor as written by the last CTA of a pass: FP64 for the
+// FP64 kernels and a float copy for the FP32 ones (which then need no FP64
+// conversion per thread).  Device buffers holding one are 16 bytes.
+struct ScaleCell {
+    double d;
+    float f;
+};
+template <typename T> __device__ __forceinline__ T load_scale(const double *p);
+template <> __device__ __forceinline__ float load_scale<float>(const double *p)
+{
+    return reinterpret_cast<const ScaleCell *>(p)->f;
+}
+template <> __device__ __forceinline__ double load_scale<double>(const double *p) { return *p; }
+__device__ __forceinline__ void store_scale(double *p, double v)
+{
+    ScaleCell *c = reinterpret_cast<ScaleCell *>(p);
+    c->d = v;
+    c->f = (float)v;
+}
 
 template <typename T> struct PassArgs {
     const vec2<T> *in;
@@ -121,27 +144,12 @@ template <typename T> struct PassArgs {
     //   adj_dLdV += dt Im(conj(g) f pre),   f = exp(-i (V + beta|pre|^2) dt)
     const vec2<T> *adj_pre;
     double *adj_dLdV;
+    // FEAT_PLANE: line g belongs to plane g / plane_lines; per plane the NL
+    // constants (FP32 split) and the prescale factor (nullable: no prescale)
+    const NLSplit *plane_nl;
+    const ScaleCell *plane_scale;
+    int plane_lines;
 };
-
-// A renormalisation factor as written by the last CTA of a pass: FP64 for the
-// FP64 kernels and a float copy for the FP32 ones (which then need no FP64
-// conversion per thread).  Device buffers holding one are 16 bytes.
-struct ScaleCell {
-    double d;
-    float f;
-};
-template <typename T> __device__ __forceinline__ T load_scale(const double *p);
-template <> __device__ __forceinline__ float load_scale<float>(const double *p)
-{
-    return reinterpret_cast<const ScaleCell *>(p)->f;
-}
-template <> __device__ __forceinline__ double load_scale<double>(const double *p) { return *p; }
-__device__ __forceinline__ void store_scale(double *p, double v)
-{
-    ScaleCell *c = reinterpret_cast<ScaleCell *>(p);
-    c->d = v;
-    c->f = (float)v;
-}
 
 // a double-word constant in shared memory: hi and lo adjacent, so one
 // 16-byte load (two for FP64) fetches both
@@ -304,6 +312,7 @@ __global__ void __launch_bounds__(PassGeom<T, XL>::THREADS, PassOcc<T, XL, MODE,
 pass_kernel(const PassArgs<T> a)
 {
     constexpr bool kNL = (FEAT & FEAT_NL) != 0, kDiag = (FEAT & FEAT_DIAG) != 0;
+    constexpr bool kPlane = (FEAT & FEAT_PLANE) != 0 && sizeof(T) == 4;
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -348,6 +357,13 @@ pass_kernel(const PassArgs<T> a)
     const int g = tile * W + w;
     const bool valid = g < a.nlines;
     const int gg = valid ? g : 0;
+    // a tile never straddles two planes (plane_lines is a multiple of W)
+    const int plane = kPlane ? gg / a.plane_lines : 0;
+    const bool tscaled = scaled || (kPlane && a.plane_scale);
+    T tscale = scale;
+    if constexpr (kPlane) {
+        if (a.plane_scale) tscale = a.plane_scale[plane].f;
+    }
     // element indices fit 32 bits (at most 256^3 cells); x lines have unit stride
     const uint32_t base = (uint32_t)((gg % a.m0) * a.s0 + (gg / a.m0) * a.s1);
     const int row = gg % a.rowmod;
@@ -400,7 +416,7 @@ pass_kernel(const PassArgs<T> a)
                 const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
                                           : sph[k];
                 v[k] = cmul2(v[k], p.hi, p.lo);
-                if (scaled) v[k] = cscale(v[k], scale);
+                if (tscaled) v[k] = cscale(v[k], tscale);
             }
             dft<N1, +1>(v);
         } else if constexpr (MODE == MODE_DIAG) {
@@ -486,7 +502,7 @@ pass_kernel(const PassArgs<T> a)
                     const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
                                               : sph[k];
                     u[k2] = cmul2(u[k2], p.hi, p.lo);
-                    if (scaled) u[k2] = cscale(u[k2], scale);
+                    if (tscaled) u[k2] = cscale(u[k2], tscale);
                 }
             }
             dft<N2, +1>(u);  // u[rr] = Z[k1][rr]
@@ -539,7 +555,8 @@ pass_kernel(const PassArgs<T> a)
         }
         if constexpr (MODE == MODE_FUSED) {
             if (kNL && a.nl_mode != NL_NONE) {
-                const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);
+                const NLConst<T> nlc =
+                    nl_const<T>(kPlane ? a.plane_nl[plane] : a.nl_split, a.nl_beta, a.nl_dt);
                 const bool imag = a.nl_mode == NL_IMAG;
                 bool done = false;
                 if constexpr (sizeof(T) == 4) {

@@ -13,15 +13,23 @@ def _lib(built_lib):
     return built_lib
 
 
-def test_batch_matches_single_runs_and_oracle(sfd, O, W):
-    runs = [W.cfg3_run(n, 77 + i) for i, n in enumerate((64, 128, 256, 64, 128, 256, 64))]
+@pytest.mark.parametrize("tuning", [None, (0, 0, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1)],
+                         ids=["autotuned", "p0", "p1", "p0-stacked", "p1-stacked"])
+def test_batch_matches_single_runs_and_oracle(sfd, O, W, tuning):
+    """Every launch choice: the persistent kernel's policies, and the 256^2
+    runs as a stack of planes through the directional pass kernels."""
+    runs = [W.cfg3_run(n, 77 + i) for i, n in enumerate((64, 128, 256, 64, 128, 256, 64, 256))]
     nsteps, dt = 40, 1e-3
     b = sfd.BatchSplit2([r["n"] for r in runs], [r["bounds"] for r in runs])
     for i, r in enumerate(runs):
         b.set_run(i, r["beta"], r["V"], r["psi"])
+    if tuning is not None:
+        b.set_tuning(*tuning)
     masses = b.step(nsteps, dt)
     tune = b.tuning()
-    assert tune["policy"] in (0, 1) and tune["order"] in (0, 1)
+    assert tune["policy"] in (0, 1) and tune["order"] in (0, 1) and tune["stack"] in (0, 1)
+    if tuning is not None:
+        assert (tune["policy"], tune["order"], tune["stack"]) == tuning
     for i, r in enumerate(runs):
         got = b.download(i)
         single = run_model(sfd, (r["n"], r["n"]), r["bounds"], r["psi"], coeffD=-0.5, beta=r["beta"], V=r["V"],
