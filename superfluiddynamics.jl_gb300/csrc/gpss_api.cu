@@ -6,8 +6,11 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <new>
 #include <string>
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/gpss.h"
 #include "gpss_internal.h"
 
@@ -97,8 +100,31 @@ static int fail(gpss_ctx *c, int code, const char *fmt, ...)
             return rc_;           \
     } while (0)
 
+// NVTX range around an entry point (profilers show the C ABI calls as ranges)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
+// Host-side fault injection for tests: with GPSS_FAULT_ALLOC=N in the
+// environment, the N-th device allocation of the process fails as if the
+// device were out of memory (no GPU fault is involved).
+static bool injected_alloc_failure()
+{
+    static const long target = [] {
+        const char *v = std::getenv("GPSS_FAULT_ALLOC");
+        return v ? std::atol(v) : 0L;
+    }();
+    static std::atomic<long> count{0};
+    return target > 0 && ++count == target;
+}
+
 static int dev_alloc(gpss_ctx *c, void **p, size_t bytes)
 {
+    if (injected_alloc_failure()) {
+        *p = nullptr;
+        return fail(c, GPSS_ENOMEM, "cudaMalloc(%zu) failed: injected by GPSS_FAULT_ALLOC", bytes);
+    }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         *p = nullptr;
@@ -1240,6 +1266,7 @@ void gpss_destroy(gpss_ctx *c)
 int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, const double *hi,
                 int precision, int flags)
 {
+    NvtxRange nvtx_("gpss_create");
     if (!out || !n || !lo || !hi) return fail(nullptr, GPSS_EINVAL, "gpss_create: null argument");
     *out = nullptr;
     if (ndim != 2 && ndim != 3) return fail(nullptr, GPSS_EINVAL, "ndim must be 2 or 3 (got %d)", ndim);
@@ -1361,6 +1388,7 @@ int gpss_set_potential(gpss_ctx *c, const double *V)
 
 int gpss_upload(gpss_ctx *c, const double *psi)
 {
+    NvtxRange nvtx_("gpss_upload");
     if (!c) return GPSS_EINVAL;
     if (!psi) return fail(c, GPSS_EINVAL, "gpss_upload: null psi");
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1378,6 +1406,7 @@ int gpss_upload(gpss_ctx *c, const double *psi)
 
 int gpss_download(gpss_ctx *c, double *psi)
 {
+    NvtxRange nvtx_("gpss_download");
     if (!c) return GPSS_EINVAL;
     if (!psi) return fail(c, GPSS_EINVAL, "gpss_download: null psi");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
@@ -1395,6 +1424,7 @@ int gpss_download(gpss_ctx *c, double *psi)
 
 int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_diag *diag)
 {
+    NvtxRange nvtx_("gpss_step");
     if (!c) return GPSS_EINVAL;
     if (nsteps < 0) return fail(c, GPSS_EINVAL, "nsteps must be >= 0");
     if (scheme != GPSS_LIE && scheme != GPSS_STRANG) return fail(c, GPSS_EINVAL, "scheme must be 1 (Lie) or 2 (Strang)");
@@ -1408,6 +1438,7 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
 
 int gpss_rk_step(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
 {
+    NvtxRange nvtx_("gpss_rk_step");
     if (!c) return GPSS_EINVAL;
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "gpss_rk_step: no field uploaded");
     if (nsteps < 0) return fail(c, GPSS_EINVAL, "gpss_rk_step: nsteps < 0");
@@ -1423,6 +1454,7 @@ int gpss_rk_step(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
 int gpss_implicit_step(gpss_ctx *c, int nsteps, int scheme, double dt, int nkrylov, double tolkrylov, int nnewton,
                        double tolnewton, int64_t *krylov_iters)
 {
+    NvtxRange nvtx_("gpss_implicit_step");
     if (!c) return GPSS_EINVAL;
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "gpss_implicit_step: no field uploaded");
     if (nsteps < 0 || nkrylov < 1 || nnewton < 1)
@@ -1439,6 +1471,7 @@ int gpss_implicit_step(gpss_ctx *c, int nsteps, int scheme, double dt, int nkryl
 
 int gpss_energy(gpss_ctx *c, double *out)
 {
+    NvtxRange nvtx_("gpss_energy");
     if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_energy: null out") : GPSS_EINVAL;
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1483,6 +1516,7 @@ int gpss_norm(gpss_ctx *c, double *out)
 
 int gpss_normalize(gpss_ctx *c)
 {
+    NvtxRange nvtx_("gpss_normalize");
     if (!c) return GPSS_EINVAL;
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1492,6 +1526,7 @@ int gpss_normalize(gpss_ctx *c)
 int gpss_ground_state(gpss_ctx *c, double dt, double tol, int64_t max_steps, int check_every,
                       double *mu_out, int64_t *steps_out)
 {
+    NvtxRange nvtx_("gpss_ground_state");
     if (!c) return GPSS_EINVAL;
     if (!(dt > 0) || !(tol > 0) || max_steps < 1 || check_every < 1)
         return fail(c, GPSS_EINVAL, "ground_state: need dt > 0, tol > 0, max_steps >= 1, check_every >= 1");
@@ -1533,6 +1568,7 @@ int gpss_device_count(void)
 int gpss_adjoint(gpss_ctx *c, const double *psi_target, int nsteps, int K, double dt, double *loss,
                  double *dLdV, double *dLdpsi0)
 {
+    NvtxRange nvtx_("gpss_adjoint");
     if (!c) return GPSS_EINVAL;
     if (!psi_target || !loss) return fail(c, GPSS_EINVAL, "gpss_adjoint: null psi_target or loss");
     if (nsteps < 1 || K < 1) return fail(c, GPSS_EINVAL, "gpss_adjoint: need nsteps >= 1 and K >= 1");
