@@ -2,7 +2,17 @@
 (oracle/gp_oracle.c), cross-checked against the independent numpy restatement
 before writing.  Each file holds the input, the FP64 oracle's output `psi`
 and the long-double oracle's output `psi_ext` (a near-exact reference: FP64
-implementations differ from it only by their own round-off).
+implementations differ from it only by their own round-off), plus traces of
+the mass and of energy(n)'s five values (E_Omega, E_Delta, E_beta, E, mu;
+GrossPitaevskii.jl:61-136) every `trace_every` steps.
+
+The cfg1..cfg4 fixtures are the seeded workloads of sfd_gb300.workloads at
+reduced sizes (the full-size fields are hundreds of MB): cfg1 at 32^3 (200
+steps), cfg2 at 32^3 (200 imaginary-time steps), two cfg3 runs at 64^2 (seeds 0 and 2, 500
+steps) and the cfg4 gradient workload at 32^2 (`cfg4_grad_32.grad.npz`: the
+loss and its directional derivatives along seeded (dV, dpsi0) directions from
+the oracle's dual-number restatement, checked here against central
+differences of the FP64 oracle).
 
 Run from the repository root on an x86 host (80-bit long double):
     python tests/golden/make_golden.py
@@ -61,14 +71,87 @@ def cases():
     c0 = importlib.import_module("sfd_gb300.workloads").cfg0()
     yield "cfg0_2d_128_1000", dict(psi0=c0["psi"], bounds=c0["bounds"], V=c0["V"], coeffD=c0["coeffD"],
                                    beta=c0["beta"], omega=0.0, nsteps=c0["nsteps"], scheme=2, imag=False,
-                                   dt=c0["dt"])
+                                   dt=c0["dt"], trace_every=100)
+    W = importlib.import_module("sfd_gb300.workloads")
+    c1 = W.cfg1(32)
+    yield "cfg1_3d_32_200", dict(psi0=c1["psi"], bounds=c1["bounds"], V=None, coeffD=c1["coeffD"],
+                                 beta=c1["beta"], omega=0.0, nsteps=c1["nsteps"], scheme=2, imag=False,
+                                 dt=c1["dt"], trace_every=20)
+    c2 = W.cfg2(32)
+    yield "cfg2_3d_32_200", dict(psi0=c2["psi"], bounds=c2["bounds"], V=c2["V"], coeffD=c2["coeffD"],
+                                 beta=c2["beta"], omega=0.0, nsteps=c2["nsteps"], scheme=2, imag=True,
+                                 dt=c2["dt"], trace_every=20)
+    # seed 1 (g = 913) is left out: at 64^2 its 500 steps amplify round-off to
+    # ~1e-9 (two FP64 restatements differ by that much), no 1e-12 parity case
+    for seed in (0, 2):
+        r = W.cfg3_run(64, seed)
+        yield f"cfg3_run_64_s{seed}", dict(psi0=r["psi"], bounds=r["bounds"], V=r["V"], coeffD=-0.5,
+                                           beta=r["beta"], omega=0.0, nsteps=500, scheme=2, imag=False,
+                                           dt=1e-3, trace_every=100, cfg3_seed=seed)
     yield "split2_3d_periodic_box", dict(psi0=np.asfortranarray(np.exp(1j * field((16, 16, 16), 4).real)),
                                          bounds=b, V=None, coeffD=-0.05 / math.sqrt(2),
                                          beta=1 / (math.sqrt(2) * 0.05), omega=0.0, nsteps=20, scheme=2,
                                          imag=False, dt=2.5e-3)
 
 
+def trace(c):
+    """(steps, mass, energies) every trace_every steps, by chunked oracle runs."""
+    every = c.get("trace_every", c["nsteps"])
+    kw = dict(coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"])
+    p = c["psi0"].copy(order="F")
+    steps, mass, en = [0], [O.c_norm(p, c["bounds"]) ** 2], [O.c_energy(p, c["bounds"], **kw)]
+    done = 0
+    while done < c["nsteps"]:
+        k = min(every, c["nsteps"] - done)
+        p = O.c_step(p, c["bounds"], nsteps=k, scheme=c["scheme"], imag=c["imag"], dt=c["dt"], **kw)
+        done += k
+        steps.append(done)
+        mass.append(O.c_norm(p, c["bounds"]) ** 2)
+        en.append(O.c_energy(p, c["bounds"], **kw))
+    return np.array(steps), np.array(mass), np.array(en), p
+
+
+def grad_case():
+    """cfg4 at 32^2, 50 steps: L and dL along 4 seeded (dV, dpsi0) directions."""
+    import importlib
+    import __graft_entry__ as g
+    g.load_package()
+    W = importlib.import_module("sfd_gb300.workloads")
+    c = W.cfg4(32)
+    nsteps = 50
+    rng = np.random.default_rng(4242)
+    dVs, dpsis, dLs = [], [], []
+    kx = np.fft.fftfreq(32)[:, None] * 32
+    ky = np.fft.fftfreq(32)[None, :] * 32
+    L = None
+    for _ in range(4):
+        a = np.fft.ifft2(np.fft.fft2(rng.standard_normal(c["shape"])) * np.exp(-(kx ** 2 + ky ** 2) / 16.0)).real
+        dv = np.asfortranarray(a / np.max(np.abs(a)))
+        dpsi = np.asfortranarray(0.1 * (rng.standard_normal(c["shape"]) + 1j * rng.standard_normal(c["shape"])))
+        L, dL = O.np_tangent_loss(c["psi"], dpsi, c["V"], dv, c["target"], c["bounds"], coeffD=c["coeffD"],
+                                  beta=c["beta"], nsteps=nsteps, dt=c["dt"])
+        dVs.append(dv)
+        dpsis.append(dpsi)
+        dLs.append(dL)
+
+    def loss(V, psi0):
+        p = O.c_step(psi0, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=V, nsteps=nsteps, dt=c["dt"])
+        z = np.sum(np.conj(c["target"]) * p) * np.prod(O.spacing(c["shape"], c["bounds"]))
+        return 1.0 - abs(z) ** 2
+
+    assert abs(loss(c["V"], c["psi"]) - L) < 1e-13
+    eps = 1e-5
+    for dv, dpsi, dL in zip(dVs, dpsis, dLs):
+        fd = (loss(c["V"] + eps * dv, c["psi"] + eps * dpsi) - loss(c["V"] - eps * dv, c["psi"] - eps * dpsi)) / (2 * eps)
+        assert abs(fd - dL) <= 1e-6 * abs(dL), (fd, dL)
+    np.savez_compressed(os.path.join(HERE, "cfg4_grad_32.grad.npz"), psi0=c["psi"], V=c["V"], target=c["target"],
+                        bounds=np.array(c["bounds"]), coeffD=c["coeffD"], beta=c["beta"], dt=c["dt"],
+                        nsteps=nsteps, L=L, dV=np.array(dVs), dpsi0=np.array(dpsis), dL=np.array(dLs))
+    print("cfg4_grad_32", "L", L, "dL", dLs)
+
+
 def main():
+    grad_case()
     for name, c in cases():
         kw = dict(coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"], nsteps=c["nsteps"],
                   scheme=c["scheme"], imag=c["imag"], dt=c["dt"])
@@ -78,7 +161,11 @@ def main():
         assert O.rel_l2(out, chk) < 4e-12, name
         e = O.c_energy(out, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"])
         V = c["V"] if c["V"] is not None else np.zeros(c["psi0"].shape)
+        steps, mass, en, tp = trace(c)
+        assert O.rel_l2(tp, out) < 1e-13, name
+        extra = {"cfg3_seed": c["cfg3_seed"]} if "cfg3_seed" in c else {}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), psi0=c["psi0"], psi=out, V=V,
+                            trace_steps=steps, trace_mass=mass, trace_energy=en, **extra,
                             has_V=c["V"] is not None, bounds=np.array(c["bounds"]), coeffD=c["coeffD"],
                             beta=c["beta"], omega=c["omega"], nsteps=c["nsteps"], scheme=c["scheme"],
                             imag=c["imag"], dt=c["dt"], energy=np.array(e), psi_ext=ext)

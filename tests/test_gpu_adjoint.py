@@ -152,3 +152,20 @@ def test_adjoint_with_rotation_vs_finite_differences(sfd, O, W):
     for dv in _directions(c["shape"], 4, seed=13):
         fd = (loss(c["V"] + eps * dv) - loss(c["V"] - eps * dv)) / (2 * eps)
         assert abs(fd - float(np.sum(dLdV * dv))) <= 1e-6 * abs(fd)
+
+
+def test_adjoint_golden_cfg4_32(sfd, W):
+    """The committed cfg4 gradient fixture (32^2, 50 steps): loss and four
+    directional derivatives from the oracle's dual-number restatement."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "cfg4_grad_32.grad.npz"))
+    b = tuple(tuple(r) for r in z["bounds"])
+    c = dict(shape=z["psi0"].shape, bounds=b, psi=z["psi0"], coeffD=float(z["coeffD"]), beta=float(z["beta"]),
+             dt=float(z["dt"]), nsteps=int(z["nsteps"]))
+    f, n = _model(sfd, c, z["V"])
+    L, dLdV, g0 = n.adjoint(z["target"], int(z["nsteps"]), 8)
+    n.close()
+    assert abs(L - float(z["L"])) < 1e-12
+    for dv, dpsi, dL in zip(z["dV"], z["dpsi0"], z["dL"]):
+        adj = float(np.sum(dLdV * dv)) + float(np.real(np.sum(np.conj(g0) * dpsi)))
+        assert abs(adj - dL) <= 1e-8 * abs(dL)

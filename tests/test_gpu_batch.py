@@ -60,3 +60,22 @@ def test_batch_repeated_calls_are_consistent(sfd, O, W):
         assert O.rel_l2(c.download(i), ref) < 1e-5
     a.close()
     c.close()
+
+
+def test_batch_golden_cfg3_runs(sfd, O):
+    """The committed cfg3 fixtures (two 64^2 runs, 500 steps) through one
+    batch, against the FP64 oracle's golden output and mass trace."""
+    import os
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    zs = [np.load(os.path.join(here, nm)) for nm in ("cfg3_run_64_s0.npz", "cfg3_run_64_s2.npz")]
+    b = sfd.BatchSplit2([z["psi0"].shape[0] for z in zs], [tuple(tuple(r) for r in z["bounds"]) for z in zs])
+    for i, z in enumerate(zs):
+        b.set_run(i, float(z["beta"]), z["V"], z["psi0"])
+    masses = b.step(int(zs[0]["nsteps"]), float(zs[0]["dt"]))
+    for i, z in enumerate(zs):
+        err = O.rel_l2(b.download(i), z["psi"])
+        print(f"cfg3 golden run {i}: rel L2 {err:.2e}")
+        assert err < 2e-5
+        cell = np.prod([(r[1] - r[0]) / m for r, m in zip(z["bounds"], z["psi0"].shape)])
+        assert abs(masses[i] * cell - z["trace_mass"][-1]) <= 1e-6 * z["trace_mass"][-1]
+    b.close()

@@ -163,7 +163,7 @@ def test_golden_fixtures_reproduce(O):
     """The committed golden vectors (tests/golden/) are what the oracle computes."""
     import os
     here = os.path.join(os.path.dirname(__file__), "golden")
-    names = sorted(f for f in os.listdir(here) if f.endswith(".npz"))
+    names = sorted(f for f in os.listdir(here) if f.endswith(".npz") and not f.endswith(".grad.npz"))
     assert names, "no golden fixtures"
     for nm in names:
         z = np.load(os.path.join(here, nm))
@@ -178,3 +178,38 @@ def test_golden_fixtures_reproduce(O):
         e = O.c_energy(z["psi"], b, coeffD=float(z["coeffD"]), beta=float(z["beta"]),
                        omega=float(z["omega"]), V=V)
         assert np.allclose(e, z["energy"], rtol=1e-12, atol=1e-14), nm
+        # the traces: chunked runs give the recorded mass and energy(n) values
+        kw = dict(coeffD=float(z["coeffD"]), beta=float(z["beta"]), omega=float(z["omega"]), V=V)
+        p = z["psi0"].copy(order="F")
+        steps = z["trace_steps"]
+        for i, s in enumerate(steps):
+            if i:
+                p = O.c_step(p, b, nsteps=int(s - steps[i - 1]), scheme=int(z["scheme"]), imag=bool(z["imag"]),
+                             dt=float(z["dt"]), **kw)
+            assert abs(O.c_norm(p, b) ** 2 - z["trace_mass"][i]) <= 1e-12 * z["trace_mass"][i], (nm, s)
+            e = np.array(O.c_energy(p, b, **kw))
+            assert np.max(np.abs(e - z["trace_energy"][i])) <= 1e-12 * np.max(np.abs(e)), (nm, s)
+
+
+def test_golden_cfg_fixtures_present():
+    """Seeded workloads 0-4 each have a golden fixture (1-3 at reduced sizes)."""
+    import os
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    names = set(os.listdir(here))
+    for nm in ("cfg0_2d_128_1000.npz", "cfg1_3d_32_200.npz", "cfg2_3d_32_200.npz", "cfg3_run_64_s0.npz",
+               "cfg3_run_64_s2.npz", "cfg4_grad_32.grad.npz"):
+        assert nm in names, nm
+
+
+def test_golden_gradient_reproduces(O):
+    """The cfg4 gradient fixture: the dual-number restatement gives the
+    recorded loss and directional derivatives."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "cfg4_grad_32.grad.npz"))
+    b = tuple(tuple(r) for r in z["bounds"])
+    for dv, dpsi, dL in zip(z["dV"], z["dpsi0"], z["dL"]):
+        L, d = O.np_tangent_loss(z["psi0"], np.asfortranarray(dpsi), z["V"], np.asfortranarray(dv), z["target"], b,
+                                 coeffD=float(z["coeffD"]), beta=float(z["beta"]), nsteps=int(z["nsteps"]),
+                                 dt=float(z["dt"]))
+        assert abs(L - float(z["L"])) < 1e-13
+        assert abs(d - dL) <= 1e-12 * abs(dL)
