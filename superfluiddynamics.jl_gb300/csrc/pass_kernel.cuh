@@ -183,9 +183,16 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #ifndef GPSS_PASS_SM_THREADS_LEAN_XL_F32
 #define GPSS_PASS_SM_THREADS_LEAN_XL_F32 896  // 7 CTAs of 128, 72 registers: x 63.8 -> 61.9 us
 #endif
+// FP64: CTAs of 64 threads.  The FP64 kernels are bound by GB300's FP64 rate
+// per SM, so small fields must spread over many SMs (2D 128^2 step 176 -> 88
+// us against 256-thread CTAs); 3D fields lose nothing (256^3 plain step 14.75
+// -> 14.38 ms, 128^3 fused 1015 -> 946 us).
+#ifndef GPSS_PASS_THREADS_F64
+#define GPSS_PASS_THREADS_F64 64
+#endif
 template <typename T, bool XL> struct PassGeom {
     static constexpr int THREADS =
-        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : GPSS_PASS_THREADS_COL_F32) : 256;
+        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : GPSS_PASS_THREADS_COL_F32) : GPSS_PASS_THREADS_F64;
 };
 template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
     static constexpr int SM_THREADS =
@@ -320,7 +327,7 @@ pass_kernel(const PassArgs<T> a)
     constexpr int N1 = S::N1, N2 = S::N2, P = S::P, W = S::W, LS = S::LS;
     constexpr int THREADS = S::THREADS;
 
-    extern __shared__ __align__(32) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     V *sdata = reinterpret_cast<V *>(smem_raw);
     DWord<V> *stw = reinterpret_cast<DWord<V> *>(sdata + S::DATA);  // stage A [N], stage B [N]
     DWord<V> *stwB = S::TWB ? stw + N : stw;
@@ -353,6 +360,17 @@ pass_kernel(const PassArgs<T> a)
     // tiles of W lines; a grid smaller than the tile count loops (the tables
     // and the reduction tail are then paid once per CTA, not once per tile)
     const int ntiles = (a.nlines + W - 1) / W;
+    // Stage A of a tile writes, and stage C reads, the same slots per thread
+    // (k1 * N2 + r for k1 < N1), and stage B's reads and writes of the tile are
+    // fenced by the barrier that precedes stage C, and the barrier after
+    // stage A keeps the next tile's stage B writes behind every thread's
+    // stage C.  So FUSED needs no barrier before a tile's stage A: one barrier
+    // for the tables is enough.  FWD and DIAG have no stage C (a fast thread's
+    // next stage A would overwrite slots another thread's stage B still
+    // reads), INV no stage A (its stage B writes slots other threads' stage C
+    // reads): they keep the barrier.
+    constexpr bool kTopBarrier = MODE != MODE_FUSED;
+    if constexpr (!kTopBarrier) __syncthreads();  // tables ready
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int g = tile * W + w;
     const bool valid = g < a.nlines;
@@ -393,7 +411,7 @@ pass_kernel(const PassArgs<T> a)
         }
         dft<N1, -1>(v);
     }
-    __syncthreads();  // tables ready; the previous tile's stage C is done with sdata
+    if constexpr (kTopBarrier) __syncthreads();  // tables ready; the previous tile's stage B is done with sdata
 
     if constexpr (N2 == 1) {
         // the whole line lives in this thread: v[k] = X[k]
