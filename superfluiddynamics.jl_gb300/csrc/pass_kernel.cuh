@@ -370,7 +370,16 @@ pass_kernel(const PassArgs<T> a)
     // reads), INV no stage A (its stage B writes slots other threads' stage C
     // reads): they keep the barrier.
     constexpr bool kTopBarrier = MODE != MODE_FUSED;
-    if constexpr (!kTopBarrier) __syncthreads();  // tables ready
+    // In the XL layout the P threads of a line are adjacent lanes of one warp
+    // (P divides 32) and only they touch the line's shared-memory slots, so
+    // the exchanges between stages need only a warp barrier.  COL lines span
+    // the CTA (lane stride W).
+    static_assert(!XL || 32 % P == 0, "an XL line must not straddle warps");
+    auto line_sync = [] {
+        if constexpr (XL) __syncwarp();
+        else __syncthreads();
+    };
+    __syncthreads();  // tables ready
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int g = tile * W + w;
     const bool valid = g < a.nlines;
@@ -411,7 +420,7 @@ pass_kernel(const PassArgs<T> a)
         }
         dft<N1, -1>(v);
     }
-    if constexpr (kTopBarrier) __syncthreads();  // tables ready; the previous tile's stage B is done with sdata
+    if constexpr (kTopBarrier) line_sync();  // the previous tile's stage B is done with sdata
 
     if constexpr (N2 == 1) {
         // the whole line lives in this thread: v[k] = X[k]
@@ -473,7 +482,7 @@ pass_kernel(const PassArgs<T> a)
                 }
                 sdata[sidx(m)] = t;
             }
-            __syncthreads();
+            line_sync();
         }
         // ---- stage B: items k1 = r + P*i
         constexpr int NI = N1 / N2;
@@ -535,7 +544,7 @@ pass_kernel(const PassArgs<T> a)
             }
         }
         if constexpr (MODE != MODE_FWD && MODE != MODE_DIAG) {
-            __syncthreads();
+            line_sync();
             // ---- stage C
 #pragma unroll
             for (int k1 = 0; k1 < N1; k1++) v[k1] = sdata[sidx(k1 * N2 + r)];
