@@ -161,9 +161,10 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 // FP32: 768 threads per SM (at most 80 registers) measured best at 256^3;
 // 1024 (64 registers) spills and runs 15-25% slower, no bound lets the fused
 // kernels grow past 85 registers and run 1.7x slower.  x lines run in CTAs
-// of 128 threads (8% faster than 256: finer barriers), y/z columns in CTAs of
-// 256 (their global accesses are W = 256/16 = 16 adjacent cells, 128 B; with
-// 128 threads they would be 64 B and run 5% slower).
+// of 128 threads (with their warp barriers 256 runs the same and 64 is 13%
+// slower), y/z columns in CTAs of 256 (their global accesses are W = 256/16 =
+// 16 adjacent cells, 128 B; with 128 threads they would be 64 B and run 5%
+// slower).
 #ifndef GPSS_PASS_THREADS_XL_F32
 #define GPSS_PASS_THREADS_XL_F32 128
 #endif
