@@ -122,18 +122,43 @@ __device__ __forceinline__ float2 nl_factor_tiny(float th)
     const float cf = fmaf(z, fmaf(z, fmaf(z, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
     return make_float2(cf, -sf);
 }
+// For |theta| <= NL_MICRO_MAX: sin to degree 3 and cos to degree 4, truncation
+// below 8e-9 absolute (a fifteenth of an FP32 ulp of the unit factor)
+#define NL_MICRO_MAX 0.0625f
+__device__ __forceinline__ float2 nl_factor_micro(float th)
+{
+    const float z = th * th;
+    const float sf = fmaf(th * z, -1.0f / 6.0f, th);
+    const float cf = fmaf(z, fmaf(z, 1.0f / 24.0f, -0.5f), 1.0f);
+    return make_float2(cf, -sf);
+}
+// exp(-i theta) for |theta| <= NL_TINY_MAX: the micro series where
+// |theta| <= NL_MICRO_MAX, else the tiny one, bitwise; branch-free (the two
+// share their Horner steps but the innermost, picked by a select), so the
+// cells of a warp do not diverge
+__device__ __forceinline__ float2 nl_factor_tiny_cell(float th)
+{
+    const bool micro = fabsf(th) <= NL_MICRO_MAX;
+    const float z = th * th;
+    const float ps = micro ? -1.0f / 6.0f : fmaf(z, 1.0f / 120.0f, -1.0f / 6.0f);
+    const float sf = fmaf(th * z, ps, th);
+    const float pc = micro ? 1.0f / 24.0f : fmaf(z, -1.0f / 720.0f, 1.0f / 24.0f);
+    const float cf = fmaf(z, fmaf(z, pc, -0.5f), 1.0f);
+    return make_float2(cf, -sf);
+}
 // exp(-i theta) for |theta| <= NL_SHORT_MAX, by the series of its size class
 __device__ __forceinline__ float2 nl_factor_short(float th)
 {
-    if (fabsf(th) <= NL_TINY_MAX) return nl_factor_tiny(th);
+    if (fabsf(th) <= NL_TINY_MAX) return nl_factor_tiny_cell(th);
     float sf, cf;
     sincos_reduced(th, &sf, &cf);
     return make_float2(cf, -sf);
 }
 // A bound on |nl_theta_short| over every cell with |psi|^2 <= rmax and
 // |V| <= vmax, with a margin far above its rounding: a warp whose bound is
-// <= NL_TINY_MAX (NL_SHORT_MAX) may call nl_factor_tiny (nl_factor_short)
-// directly and still produce exactly what nl_factor gives cell by cell.
+// <= NL_MICRO_MAX (NL_TINY_MAX, NL_SHORT_MAX) may call nl_factor_micro
+// (nl_factor_tiny_cell, nl_factor_short) directly and still produce exactly
+// what nl_factor gives cell by cell.
 __device__ __forceinline__ float nl_theta_bound(float rmax, float vmax, const NLConst<float> &c)
 {
     return (fabsf(c.bdh) * rmax + fabsf(c.dh) * vmax) * 1.001f;
