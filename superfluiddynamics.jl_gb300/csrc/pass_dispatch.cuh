@@ -41,8 +41,19 @@ static cudaError_t launch_pass_inst(const PassArgs<T> &a, int tiles, cudaStream_
         if (dev >= 0 && dev < 64) wave[dev] = grid_cap;
     }
     const int grid = tiles < grid_cap ? tiles : grid_cap;
-    k<<<grid, S::THREADS, S::SMEM_BYTES, s>>>(a);
-    return cudaGetLastError();
+    // programmatic stream serialization: the kernel waits for the previous
+    // grid itself (griddepcontrol.wait) after loading its constant tables
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(S::THREADS);
+    cfg.dynamicSmemBytes = S::SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, a);
 }
 
 template <typename T, int N, bool XL>

@@ -351,6 +351,10 @@ pass_kernel(const PassArgs<T> a)
         else return q * W + w;
     };
 
+    // Programmatic dependent launch: a pass may start while the previous
+    // kernel of the stream finishes; only the constant tables above are read
+    // before the previous grid has completed and its writes are visible.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const bool scaled = a.scale != nullptr;
     const T scale = scaled ? load_scale<T>(a.scale) : (T)1;
     const T kmult = a.kmult;
@@ -684,6 +688,12 @@ pass_kernel(const PassArgs<T> a)
     }
 
     }  // tiles
+
+    // This CTA's tiles are done: the next kernel of the stream may be
+    // scheduled once every CTA has got here (so all of this grid's CTAs have
+    // been resident: the dependent grid cannot hold SM slots this one needs),
+    // overlapping its launch and table loads with this grid's tail.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
         if (red) {
