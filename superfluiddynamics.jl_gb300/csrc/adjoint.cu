@@ -9,6 +9,7 @@
 //     g_in = conj(f) g + 2 beta dt Im(conj(g) psi_out) psi_in,
 //     dL/dV += dt Im(conj(g) psi_out)          (per cell, accumulated in FP64).
 #include "gpss_internal.h"
+#include "pdl.cuh"
 
 namespace gpss {
 
@@ -26,6 +27,7 @@ template <typename T>
 __global__ void k_overlap(const vec2<T> *__restrict__ a, const vec2<T> *__restrict__ b, int64_t total,
                           double *__restrict__ partials)
 {
+    pdl_enter();
     __shared__ double sr[256], si[256];
     double re = 0.0, im = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
@@ -53,6 +55,7 @@ __global__ void k_overlap(const vec2<T> *__restrict__ a, const vec2<T> *__restri
 // z = dV * sum of the partials (fixed order), one CTA
 __global__ void k_overlap_finish(const double *__restrict__ partials, int nblocks, double dV, double *__restrict__ z)
 {
+    pdl_enter();
     __shared__ double sr[256], si[256];
     double re = 0.0, im = 0.0;
     for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
@@ -80,10 +83,10 @@ cudaError_t launch_overlap(const vec2<T> *a, const vec2<T> *b, int64_t total, do
                            double *z, cudaStream_t s)
 {
     const int blocks = grid_for(total, 256);
-    k_overlap<T><<<blocks, 256, 0, s>>>(a, b, total, partials);
+    launch_pdl(k_overlap<T>, dim3(blocks), dim3(256), 0, s, a, b, total, partials);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_overlap_finish<<<1, 256, 0, s>>>(partials, blocks, dV, z);
+    launch_pdl(k_overlap_finish, dim3(1), dim3(256), 0, s, partials, blocks, dV, z);
     return cudaGetLastError();
 }
 
@@ -92,6 +95,7 @@ template <typename T>
 __global__ void k_seed(vec2<T> *__restrict__ g, const vec2<T> *__restrict__ target, const double *__restrict__ z,
                        double dV, int64_t total)
 {
+    pdl_enter();
     const double zr = -2.0 * dV * z[0], zi = -2.0 * dV * z[1];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -104,7 +108,7 @@ template <typename T>
 cudaError_t launch_seed(vec2<T> *g, const vec2<T> *target, const double *z, double dV, int64_t total,
                         cudaStream_t s)
 {
-    k_seed<T><<<grid_for(total, 256), 256, 0, s>>>(g, target, z, dV, total);
+    launch_pdl(k_seed<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, g, target, z, dV, total);
     return cudaGetLastError();
 }
 
@@ -113,6 +117,7 @@ template <typename T>
 __global__ void k_nl_adjoint(vec2<T> *__restrict__ g, const vec2<T> *__restrict__ psi_in, const T *__restrict__ V,
                              double *__restrict__ dLdV, double beta, double dt, int64_t total)
 {
+    pdl_enter();
     const NLConst<T> c(beta, dt);
     const T two_beta_dt = (T)(2.0 * beta * dt);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
@@ -133,7 +138,7 @@ template <typename T>
 cudaError_t launch_nl_adjoint(vec2<T> *g, const vec2<T> *psi_in, const T *V, double *dLdV, double beta, double dt,
                               int64_t total, cudaStream_t s)
 {
-    k_nl_adjoint<T><<<grid_for(total, 256), 256, 0, s>>>(g, psi_in, V, dLdV, beta, dt, total);
+    launch_pdl(k_nl_adjoint<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, g, psi_in, V, dLdV, beta, dt, total);
     return cudaGetLastError();
 }
 

@@ -4,6 +4,7 @@
 // from the fused directional passes (the host chains them); everything else of
 // a Krylov iteration is here.
 #include "gpss_internal.h"
+#include "pdl.cuh"
 
 namespace gpss {
 
@@ -28,6 +29,7 @@ __global__ void k_im_prep_be(const vec2<T> *__restrict__ phi, const T *__restric
                              double dt, int scheme, vec2<T> *__restrict__ M, T *__restrict__ Anl,
                              vec2<T> *__restrict__ b, int64_t total)
 {
+    pdl_enter();
     GRID_LOOP(e, total) {
         const vec2<T> p = phi[e];
         const T vv = V ? V[e] : (T)0;
@@ -52,6 +54,7 @@ __global__ void k_im_prep_cn(const vec2<T> *__restrict__ phi, const vec2<T> *__r
                              vec2<T> *__restrict__ psim, T *__restrict__ Anl, vec2<T> *__restrict__ Anl2,
                              vec2<T> *__restrict__ M, int64_t total)
 {
+    pdl_enter();
     const bool newton = scheme == IM_SCHEME_CN || scheme == IM_SCHEME_CN_T;
     const bool tsch = scheme == IM_SCHEME_CN_T || scheme == IM_SCHEME_CN_QN_T;
     const T bt = (T)beta;
@@ -82,6 +85,7 @@ __global__ void k_im_rhs_cn(const vec2<T> *__restrict__ phi, const vec2<T> *__re
                             const T *__restrict__ V, double beta, double idt, int tsch, vec2<T> *__restrict__ b,
                             int64_t total)
 {
+    pdl_enter();
     GRID_LOOP(e, total) {
         const vec2<T> q = psim[e], L = lap[e], a = phi1[e], p = phi[e];
         const T f = (V ? V[e] : (T)0) + (T)beta * (q.x * q.x + q.y * q.y);
@@ -101,6 +105,7 @@ __global__ void k_im_op(const vec2<T> *__restrict__ x, const vec2<T> *__restrict
                         const vec2<T> *__restrict__ M, const T *__restrict__ Anl, const vec2<T> *__restrict__ Anl2,
                         const vec2<T> *__restrict__ b, int precond, vec2<T> *__restrict__ out, int64_t total)
 {
+    pdl_enter();
     const T id = (T)idt, h = (T)0.5;
     GRID_LOOP(e, total) {
         const vec2<T> v = x[e], L = lap[e];
@@ -165,6 +170,7 @@ __global__ void k_im_dot2(const vec2<T> *__restrict__ a1, const vec2<T> *__restr
                           const vec2<T> *__restrict__ a2, const vec2<T> *__restrict__ b2, int64_t total,
                           double *__restrict__ partials)
 {
+    pdl_enter();
     __shared__ double s1[256], s2[256];
     double x1 = 0.0, x2 = 0.0;
     GRID_LOOP(e, total) {
@@ -194,6 +200,7 @@ __global__ void k_im_dot2(const vec2<T> *__restrict__ a1, const vec2<T> *__restr
 // out[0..1] = the sums of the partials (fixed order), one CTA
 __global__ void k_im_dot_finish(const double *__restrict__ partials, int nblocks, double *__restrict__ out)
 {
+    pdl_enter();
     __shared__ double s1[256], s2[256];
     double x1 = 0.0, x2 = 0.0;
     for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
@@ -221,6 +228,7 @@ template <typename T>
 __global__ void k_im_axmy(vec2<T> *__restrict__ out, const vec2<T> *__restrict__ x, double alpha,
                           const vec2<T> *__restrict__ y, int64_t total)
 {
+    pdl_enter();
     const T a = (T)alpha;
     GRID_LOOP(e, total) {
         const vec2<T> u = x[e], w = y[e];
@@ -234,6 +242,7 @@ __global__ void k_im_update(vec2<T> *__restrict__ phi, const vec2<T> *__restrict
                             const vec2<T> *__restrict__ As, vec2<T> *__restrict__ r, double alpha, double omega,
                             int64_t total)
 {
+    pdl_enter();
     const T a = (T)alpha, w = (T)omega;
     GRID_LOOP(e, total) {
         const vec2<T> f = phi[e], pp = p[e], ss = s[e], aa = As[e];
@@ -247,6 +256,7 @@ template <typename T>
 __global__ void k_im_pdir(vec2<T> *__restrict__ p, const vec2<T> *__restrict__ r, const vec2<T> *__restrict__ Ap,
                           double beta, double omega, int64_t total)
 {
+    pdl_enter();
     const T bt = (T)beta, w = (T)omega;
     GRID_LOOP(e, total) {
         const vec2<T> pp = p[e], rr = r[e], aa = Ap[e];
@@ -260,6 +270,7 @@ template <typename T>
 __global__ void k_im_mfield(vec2<T> *__restrict__ out, const vec2<T> *__restrict__ M, const vec2<T> *__restrict__ x,
                             int64_t total)
 {
+    pdl_enter();
     GRID_LOOP(e, total) {
         const vec2<T> m = M[e], v = x[e];
         out[e] = mk<vec2<T>>(m.x * v.x - m.y * v.y, m.x * v.y + m.y * v.x);
@@ -271,7 +282,7 @@ __global__ void k_im_mfield(vec2<T> *__restrict__ out, const vec2<T> *__restrict
 template <typename T>
 cudaError_t im_mfield(vec2<T> *out, const vec2<T> *M, const vec2<T> *x, int64_t total, cudaStream_t s)
 {
-    k_im_mfield<T><<<im_grid(total), 256, 0, s>>>(out, M, x, total);
+    launch_pdl(k_im_mfield<T>, dim3(im_grid(total)), dim3(256), 0, s, out, M, x, total);
     return cudaGetLastError();
 }
 
@@ -279,7 +290,7 @@ template <typename T>
 cudaError_t im_prep_be(const vec2<T> *phi, const T *V, double beta, double dt, int scheme, vec2<T> *M, T *Anl,
                        vec2<T> *b, int64_t total, cudaStream_t s)
 {
-    k_im_prep_be<T><<<im_grid(total), 256, 0, s>>>(phi, V, beta, 1.0 / dt, dt, scheme, M, Anl, b, total);
+    launch_pdl(k_im_prep_be<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, V, beta, 1.0 / dt, dt, scheme, M, Anl, b, total);
     return cudaGetLastError();
 }
 
@@ -287,7 +298,7 @@ template <typename T>
 cudaError_t im_prep_cn(const vec2<T> *phi, const vec2<T> *phi1, const T *V, double beta, double dt, int scheme,
                        vec2<T> *psim, T *Anl, vec2<T> *Anl2, vec2<T> *M, int64_t total, cudaStream_t s)
 {
-    k_im_prep_cn<T><<<im_grid(total), 256, 0, s>>>(phi, phi1, V, beta, 1.0 / dt, scheme, psim, Anl, Anl2, M, total);
+    launch_pdl(k_im_prep_cn<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, phi1, V, beta, 1.0 / dt, scheme, psim, Anl, Anl2, M, total);
     return cudaGetLastError();
 }
 
@@ -295,7 +306,7 @@ template <typename T>
 cudaError_t im_rhs_cn(const vec2<T> *phi, const vec2<T> *phi1, const vec2<T> *psim, const vec2<T> *lap, const T *V,
                       double beta, double dt, int tsch, vec2<T> *b, int64_t total, cudaStream_t s)
 {
-    k_im_rhs_cn<T><<<im_grid(total), 256, 0, s>>>(phi, phi1, psim, lap, V, beta, 1.0 / dt, tsch, b, total);
+    launch_pdl(k_im_rhs_cn<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, phi1, psim, lap, V, beta, 1.0 / dt, tsch, b, total);
     return cudaGetLastError();
 }
 
@@ -303,7 +314,7 @@ template <typename T>
 cudaError_t im_op(const vec2<T> *x, const vec2<T> *lap, int scheme, double dt, const vec2<T> *M, const T *Anl,
                   const vec2<T> *Anl2, const vec2<T> *b, int precond, vec2<T> *out, int64_t total, cudaStream_t s)
 {
-    k_im_op<T><<<im_grid(total), 256, 0, s>>>(x, lap, scheme, 1.0 / dt, M, Anl, Anl2, b, precond, out, total);
+    launch_pdl(k_im_op<T>, dim3(im_grid(total)), dim3(256), 0, s, x, lap, scheme, 1.0 / dt, M, Anl, Anl2, b, precond, out, total);
     return cudaGetLastError();
 }
 
@@ -312,17 +323,17 @@ cudaError_t im_dot2(const vec2<T> *a1, const vec2<T> *b1, const vec2<T> *a2, con
                     double *partials, double *out, cudaStream_t s)
 {
     const int g = im_grid(total);
-    k_im_dot2<T><<<g, 256, 0, s>>>(a1, b1, a2, b2, total, partials);
+    launch_pdl(k_im_dot2<T>, dim3(g), dim3(256), 0, s, a1, b1, a2, b2, total, partials);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_im_dot_finish<<<1, 256, 0, s>>>(partials, g, out);
+    launch_pdl(k_im_dot_finish, dim3(1), dim3(256), 0, s, partials, g, out);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t im_axmy(vec2<T> *out, const vec2<T> *x, double alpha, const vec2<T> *y, int64_t total, cudaStream_t s)
 {
-    k_im_axmy<T><<<im_grid(total), 256, 0, s>>>(out, x, alpha, y, total);
+    launch_pdl(k_im_axmy<T>, dim3(im_grid(total)), dim3(256), 0, s, out, x, alpha, y, total);
     return cudaGetLastError();
 }
 
@@ -330,7 +341,7 @@ template <typename T>
 cudaError_t im_update(vec2<T> *phi, const vec2<T> *p, const vec2<T> *sv, const vec2<T> *As, vec2<T> *r, double alpha,
                       double omega, int64_t total, cudaStream_t s)
 {
-    k_im_update<T><<<im_grid(total), 256, 0, s>>>(phi, p, sv, As, r, alpha, omega, total);
+    launch_pdl(k_im_update<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, p, sv, As, r, alpha, omega, total);
     return cudaGetLastError();
 }
 
@@ -338,7 +349,7 @@ template <typename T>
 cudaError_t im_pdir(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, double beta, double omega, int64_t total,
                     cudaStream_t s)
 {
-    k_im_pdir<T><<<im_grid(total), 256, 0, s>>>(p, r, Ap, beta, omega, total);
+    launch_pdl(k_im_pdir<T>, dim3(im_grid(total)), dim3(256), 0, s, p, r, Ap, beta, omega, total);
     return cudaGetLastError();
 }
 

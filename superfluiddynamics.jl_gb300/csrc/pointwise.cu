@@ -2,6 +2,7 @@
 // boundary, the plain-form phase multiply and nonlinear step, and the
 // scaling that applies a renormalisation factor left on the device.
 #include "gpss_internal.h"
+#include "pdl.cuh"
 
 namespace gpss {
 
@@ -16,6 +17,7 @@ static int grid_for(int64_t count, int threads)
 
 __global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ out, int64_t count)
 {
+    pdl_enter();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
          i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (float)in[i];
@@ -23,6 +25,7 @@ __global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ 
 
 __global__ void k_f32_to_f64(const float *__restrict__ in, double *__restrict__ out, int64_t count)
 {
+    pdl_enter();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
          i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (double)in[i];
@@ -30,13 +33,13 @@ __global__ void k_f32_to_f64(const float *__restrict__ in, double *__restrict__ 
 
 cudaError_t launch_f64_to_f32(const double *in, float *out, int64_t count, cudaStream_t s)
 {
-    k_f64_to_f32<<<grid_for(count, 256), 256, 0, s>>>(in, out, count);
+    launch_pdl(k_f64_to_f32, dim3(grid_for(count, 256)), dim3(256), 0, s, in, out, count);
     return cudaGetLastError();
 }
 
 cudaError_t launch_f32_to_f64(const float *in, double *out, int64_t count, cudaStream_t s)
 {
-    k_f32_to_f64<<<grid_for(count, 256), 256, 0, s>>>(in, out, count);
+    launch_pdl(k_f32_to_f64, dim3(grid_for(count, 256)), dim3(256), 0, s, in, out, count);
     return cudaGetLastError();
 }
 
@@ -47,6 +50,7 @@ template <typename T>
 __global__ void k_mul_phase(vec2<T> *__restrict__ data, const vec2<T> *__restrict__ phase,
                             int64_t prow, int axis, int64_t nx, int64_t ny, int64_t nk, int64_t total)
 {
+    pdl_enter();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         int64_t k, row;
@@ -62,7 +66,7 @@ template <typename T>
 cudaError_t launch_mul_phase(vec2<T> *data, const vec2<T> *phase, int64_t prow, int axis,
                              const int64_t *n, int64_t total, cudaStream_t s)
 {
-    k_mul_phase<T><<<grid_for(total, 256), 256, 0, s>>>(data, phase, prow, axis, n[0], n[1], n[axis],
+    launch_pdl(k_mul_phase<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, data, phase, prow, axis, n[0], n[1], n[axis],
                                                         total);
     return cudaGetLastError();
 }
@@ -72,6 +76,7 @@ template <typename T>
 __global__ void k_nl(vec2<T> *__restrict__ psi, const T *__restrict__ V, double beta, double dt,
                      int imag, int64_t total)
 {
+    pdl_enter();
     const NLConst<T> c(beta, dt);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -84,13 +89,14 @@ template <typename T>
 cudaError_t launch_nl(vec2<T> *psi, const T *V, double beta, double dt, int imag, int64_t total,
                       cudaStream_t s)
 {
-    k_nl<T><<<grid_for(total, 256), 256, 0, s>>>(psi, V, beta, dt, imag, total);
+    launch_pdl(k_nl<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, psi, V, beta, dt, imag, total);
     return cudaGetLastError();
 }
 
 template <typename T>
 __global__ void k_scale(vec2<T> *__restrict__ psi, const double *__restrict__ scale, int64_t total)
 {
+    pdl_enter();
     const T s = (T)(*scale);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x)
@@ -100,7 +106,7 @@ __global__ void k_scale(vec2<T> *__restrict__ psi, const double *__restrict__ sc
 template <typename T>
 cudaError_t launch_scale(vec2<T> *psi, const double *scale, int64_t total, cudaStream_t s)
 {
-    k_scale<T><<<grid_for(total, 256), 256, 0, s>>>(psi, scale, total);
+    launch_pdl(k_scale<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, psi, scale, total);
     return cudaGetLastError();
 }
 
@@ -111,6 +117,7 @@ template <typename T>
 __global__ void k_nl_term(const vec2<T> *__restrict__ q, const T *__restrict__ V, T beta, vec2<T> *__restrict__ t,
                           int64_t total)
 {
+    pdl_enter();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const vec2<T> v = q[e];
@@ -122,7 +129,7 @@ __global__ void k_nl_term(const vec2<T> *__restrict__ q, const T *__restrict__ V
 template <typename T>
 cudaError_t launch_nl_term(const vec2<T> *q, const T *V, double beta, vec2<T> *t, int64_t total, cudaStream_t s)
 {
-    k_nl_term<T><<<grid_for(total, 256), 256, 0, s>>>(q, V, (T)beta, t, total);
+    launch_pdl(k_nl_term<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, q, V, (T)beta, t, total);
     return cudaGetLastError();
 }
 
@@ -135,6 +142,7 @@ template <typename T>
 __global__ void k_mask_spectrum(vec2<T> *__restrict__ f, const int *__restrict__ lim, int64_t n_last, int64_t inner,
                                 int64_t total)
 {
+    pdl_enter();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t il = e / inner;
@@ -147,7 +155,7 @@ template <typename T>
 cudaError_t launch_mask_spectrum(vec2<T> *f, const int *lim, int64_t n_last, int64_t inner, int64_t total,
                                  cudaStream_t s)
 {
-    k_mask_spectrum<T><<<grid_for(total, 256), 256, 0, s>>>(f, lim, n_last, inner, total);
+    launch_pdl(k_mask_spectrum<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, f, lim, n_last, inner, total);
     return cudaGetLastError();
 }
 
@@ -159,6 +167,7 @@ template <typename T>
 __global__ void k_rk_combine(const vec2<T> *__restrict__ k, const vec2<T> *__restrict__ t, const vec2<T> *psi0,
                              vec2<T> *acc, vec2<T> *out, int acc_mode, T acc_w, T cf, int from_acc, int64_t total)
 {
+    pdl_enter();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const vec2<T> a = k[e], b = t[e];
@@ -181,7 +190,7 @@ template <typename T>
 cudaError_t launch_rk_combine(const vec2<T> *k, const vec2<T> *t, const vec2<T> *psi0, vec2<T> *acc, vec2<T> *out,
                               int acc_mode, double acc_w, double cf, int from_acc, int64_t total, cudaStream_t s)
 {
-    k_rk_combine<T><<<grid_for(total, 256), 256, 0, s>>>(k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc,
+    launch_pdl(k_rk_combine<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc,
                                                          total);
     return cudaGetLastError();
 }
