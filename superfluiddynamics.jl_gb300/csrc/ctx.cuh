@@ -372,7 +372,7 @@ static bool pipe_ok(const gpss_ctx *c, int axis)
 
 template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const PassArgs<T> &a)
 {
-    if (mode == MODE_FUSED && !a.acc && pipe_ok(c, axis)) {
+    if (mode == MODE_FUSED && !a.acc && !a.nl_pre && !a.dot_with && pipe_ok(c, axis)) {
         const int ntiles = (int)(c->total / c->n[axis] / (4096 / c->n[axis]));
         cudaError_t e = PassLauncher<T>::pipe(axis == 0, (int)c->n[axis], a, ntiles, c->stream);
         if (e != cudaSuccess)

@@ -83,6 +83,80 @@ template <typename T> static int energy_impl(gpss_ctx *c, double *out, double *m
     return GPSS_OK;
 }
 
+// One kinetic flow L(dtl) in imaginary time as passes x, y[, z] for the
+// merged step below: the first pass reads `in0` and may carry the nonlinear
+// prologue (chi = N(dtnl)(c->scale * psi), stored to chi_out when non-null),
+// the last pass writes `out_last` and may carry the nonlinear epilogue, the
+// inner product with `dot_with` in place of the mass sum, and a finish.
+template <typename T>
+static int imag_flow(gpss_ctx *c, double dtl, const void *in0, bool pre_nl, void *chi_out, double dtnl,
+                     bool nl_last, void *out_last, const void *dot_with, int red_last, int fin_last)
+{
+    for (int axis = 0; axis < c->ndim; axis++) {
+        const bool first = axis == 0, last = axis == c->ndim - 1;
+        PassArgs<T> a = axis_args<T>(c, axis, first ? in0 : c->psi, last ? out_last : c->psi);
+        const void *ph;
+        GPSS_TRY(get_phase(c, axis, dtl, 1, 1, &ph, &a.prow));
+        a.phase = (const vec2<T> *)ph;
+        if ((first && pre_nl) || (last && nl_last)) {
+            a.V = c->have_V ? (const T *)c->V : nullptr;
+            a.nl_beta = c->beta;
+            a.nl_dt = dtnl;
+            a.nl_split = nl_split(c->beta, dtnl);
+        }
+        if (first && pre_nl) {
+            a.nl_pre = 1;
+            a.scale = c->scale;
+            a.nl_pre_out = (vec2<T> *)chi_out;
+        }
+        if (last) {
+            if (nl_last) a.nl_mode = NL_IMAG;
+            a.dot_with = (const vec2<T> *)dot_with;
+            a.red |= red_last;
+        }
+        if (a.red) set_finish<T>(c, a, axis, last ? fin_last : FIN_NONE);
+        GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
+    }
+    return GPSS_OK;
+}
+
+// Imaginary time, Strang, Omega = 0, fused forms.  With chi_n = N L(dt/2)
+// psi_n and the step psi_{n+1} = c_n L(dt/2) chi_n (c_n the unit-mass
+// factor of normalize!, Fields.jl:196-200):
+//     chi_{n+1} = N(c_n L(dt) chi_n),   c_n^-2 = <chi_n, L(dt) chi_n> dV,
+// because L(dt/2) is real, positive and self-adjoint on the spectrum, so
+// ||L(dt/2) chi||^2 = <chi, L(dt) chi>.  One kinetic flow per step instead of
+// two: chi_n is kept in the scratch buffer for the inner product of the last
+// pass, and N with the factor c_n runs as the prologue of the next first
+// pass.  The sequence is L(dt/2) N | [L(dt) <.,.> | c N]^(n-1) | L(dt/2) |.|.
+template <typename T> static int imag_merged(gpss_ctx *c, int nsteps, double dt)
+{
+    void *chi = c->scratch;
+    GPSS_TRY(imag_flow<T>(c, dt * 0.5, c->psi, false, nullptr, dt, true, chi, nullptr, 0, FIN_NONE));
+    auto full = [&](bool first) -> int {
+        return imag_flow<T>(c, dt, first ? chi : c->psi, !first, chi, dt, false, c->psi, chi, RED_MASS,
+                            FIN_UNITMASS);
+    };
+    int s = 1;
+    if (s < nsteps) {
+        GPSS_TRY(full(true));
+        s++;
+    }
+    if (c->total <= kGraphCells) {
+        const std::string key = graph_key("imag", {dt, (double)kGraphChunk});
+        for (; s + kGraphChunk <= nsteps; s += kGraphChunk)
+            GPSS_TRY(graph_run(c, key, [&]() -> int {
+                for (int i = 0; i < kGraphChunk; i++) GPSS_TRY(full(false));
+                return GPSS_OK;
+            }));
+    }
+    for (; s < nsteps; s++) GPSS_TRY(full(false));
+    // the last half step: psi_n = c L(dt/2) chi, c from its own mass
+    GPSS_TRY(imag_flow<T>(c, dt * 0.5, nsteps == 1 ? chi : c->psi, nsteps > 1, nullptr, dt, false, c->psi,
+                          nullptr, RED_MASS, FIN_UNITMASS));
+    return apply_scale<T>(c);
+}
+
 template <typename T>
 static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_diag *diag)
 {
@@ -145,6 +219,8 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         // with the other axes' derivatives when Omega = 0)
         GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, diag ? RED_POINT : 0, diag != nullptr, lock));
         diag_done = diag != nullptr;
+    } else if (imag && scheme == GPSS_STRANG && c->omega == 0.0 && !(c->flags & GPSS_FLAG_NOMERGE)) {
+        GPSS_TRY(imag_merged<T>(c, nsteps, dt));
     } else if (imag) {
         for (int s = 0; s < nsteps; s++) {
             const bool pre = s > 0;

@@ -65,6 +65,10 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
         const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr ||
                           a.pre_out != nullptr || a.adj_pre != nullptr;
         const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
+        if (a.nl_pre || a.dot_with) {
+            if (diag || a.nl_mode != NL_NONE) return cudaErrorInvalidValue;
+            return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_IMAGM>(a, blocks, s);
+        }
         if constexpr (sizeof(T) == 4 && N >= 64) {
             if (a.plane_nl || a.plane_scale) {
                 if (diag) return cudaErrorInvalidValue;  // planes carry no energy sums or rotation

@@ -74,7 +74,11 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //   FEAT_PLANE a stack of independent 2D runs of one shape (planes): the
 //              nonlinear constants and the deferred renormalisation factor
 //              are per plane (plane_nl, plane_scale)
-enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4 };
+//   FEAT_IMAGM the merged imaginary-time step: the nonlinear flow as a
+//              prologue of the first pass (nl_pre, after the deferred
+//              factor, its result also stored to nl_pre_out) and the mass sum
+//              of the last pass replaced by Re sum conj(dot_with) psi
+enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -149,6 +153,12 @@ template <typename T> struct PassArgs {
     const NLSplit *plane_nl;
     const ScaleCell *plane_scale;
     int plane_lines;
+    // FEAT_IMAGM: psi_in <- N(scale * psi_in) before the transform (imaginary
+    // time; constants nl_beta/nl_dt/nl_split, V), stored to nl_pre_out
+    // (nullable); and RED_MASS sums Re(conj(dot_with) psi_out) (nullable)
+    int nl_pre;
+    vec2<T> *nl_pre_out;
+    const vec2<T> *dot_with;
 };
 
 // a double-word constant in shared memory: hi and lo adjacent, so one
@@ -321,7 +331,8 @@ pass_kernel(const PassArgs<T> a)
 {
     constexpr bool kNL = (FEAT & FEAT_NL) != 0, kDiag = (FEAT & FEAT_DIAG) != 0;
     constexpr bool kPlane = (FEAT & FEAT_PLANE) != 0 && sizeof(T) == 4;
-    const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag ? RED_MASS : 0));
+    constexpr bool kImagM = (FEAT & FEAT_IMAGM) != 0;
+    const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
     using S = PassShape<T, N, XL>;
@@ -391,7 +402,8 @@ pass_kernel(const PassArgs<T> a)
     const int gg = valid ? g : 0;
     // a tile never straddles two planes (plane_lines is a multiple of W)
     const int plane = kPlane ? gg / a.plane_lines : 0;
-    const bool tscaled = scaled || (kPlane && a.plane_scale);
+    // (the imaginary-time prologue applies the factor itself, before N)
+    const bool tscaled = (scaled && !(kImagM && a.nl_pre)) || (kPlane && a.plane_scale);
     T tscale = scale;
     if constexpr (kPlane) {
         if (a.plane_scale) tscale = a.plane_scale[plane].f;
@@ -410,6 +422,18 @@ pass_kernel(const PassArgs<T> a)
             if (!valid) {  // ... and sum nothing
 #pragma unroll
                 for (int j = 0; j < N1; j++) v[j] = mk<V>((T)0, (T)0);
+            }
+        }
+        if constexpr (MODE == MODE_FUSED && kImagM) {
+            if (a.nl_pre) {  // chi = N(scale * psi), kept for the inner product of the last pass
+                const NLConst<T> nlc = nl_const<T>(a.nl_split, a.nl_beta, a.nl_dt);
+#pragma unroll
+                for (int j = 0; j < N1; j++) {
+                    const uint32_t e = base + (uint32_t)(r + N2 * j) * st;
+                    const V u = scaled ? cscale(v[j], scale) : v[j];
+                    v[j] = nl_apply(u, a.V ? a.V[e] : (T)0, nlc, true);
+                    if (valid && a.nl_pre_out) a.nl_pre_out[e] = v[j];
+                }
             }
         }
         if constexpr (MODE == MODE_DIAG) {
@@ -664,8 +688,16 @@ pass_kernel(const PassArgs<T> a)
                     if (a.V) acc_pot += a.V[base + (uint32_t)(r + N2 * j) * st] * rho;
                 }
             } else if (red & RED_MASS) {
+                if (kImagM && a.dot_with) {
 #pragma unroll
-                for (int j = 0; j < N1; j++) acc_mass += v[j].x * v[j].x + v[j].y * v[j].y;
+                    for (int j = 0; j < N1; j++) {
+                        const V w = a.dot_with[base + (uint32_t)(r + N2 * j) * st];
+                        acc_mass += w.x * v[j].x + w.y * v[j].y;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < N1; j++) acc_mass += v[j].x * v[j].x + v[j].y * v[j].y;
+                }
             }
         }
         if (valid) {

@@ -270,6 +270,30 @@ def test_cfg1_fullsize_fp32_vs_fp64(sfd, O, W):
     assert abs(d["energy"][3] - e0[3]) / abs(e0[3]) < 1e-3
 
 
+@pytest.mark.parametrize("nsteps,per_call", [(1, None), (2, None), (3, 1), (40, None), (70, 33)])
+@pytest.mark.parametrize("shape", [(64, 32), (16, 8, 32)])
+def test_merged_imaginary_time(sfd, O, shape, nsteps, per_call):
+    """Imaginary-time Strang with Omega = 0 takes one kinetic flow per step
+    (renormalisation from <chi, L(dt) chi>, the nonlinear stage as the next
+    pass's prologue): FP64 against the oracle and against the unmerged
+    sequence, FP32 against the oracle; calls of one step and chunks that
+    cross the graph-captured blocks of 32 steps."""
+    nd = len(shape)
+    bounds = tuple((-6.0, 6.0 + a) for a in range(nd))
+    psi0 = random_field(shape, seed=11)
+    V = O.quadratic_potential(shape, bounds)
+    kw = dict(coeffD=-0.5, beta=40.0, V=V, dt=1e-2, nsteps=nsteps, imag=True, per_call=per_call)
+    ref = O.c_step(psi0, bounds, coeffD=-0.5, beta=40.0, V=V, nsteps=nsteps, imag=True, dt=1e-2)
+    got = run_model(sfd, shape, bounds, psi0, **kw)
+    unmerged = run_model(sfd, shape, bounds, psi0, merge=False, **kw)
+    assert O.rel_l2(got, ref) < TOL64
+    assert O.rel_l2(got, unmerged) < TOL64
+    dV = np.prod([(b[1] - b[0]) / n for n, b in zip(shape, bounds)])
+    assert abs(np.sum(np.abs(got) ** 2) * dV - 1.0) < 1e-12
+    got32 = run_model(sfd, shape, bounds, psi0, precision="fp32", **kw)
+    assert O.rel_l2(got32, ref) < TOL32
+
+
 def test_cfg2_ground_state_small(sfd, O, W):
     """Imaginary time (cfg2 physics at 32^3): FP32 stages with FP64 reductions
     track the FP64 oracle; mu agrees."""
