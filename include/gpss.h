@@ -46,6 +46,13 @@ extern "C" {
 #define GPSS_FLAG_PIPE 8      /* x passes through the persistent asynchronous-copy
                                  pipeline (same arithmetic; the direct kernel is
                                  faster on GB300 and is the default) */
+#define GPSS_FLAG_ENERGY_CACHE 16 /* real-time Strang with Omega = 0 (fused, merged):
+                                 every gpss_step also measures the energies of its
+                                 final field in its last passes, and gpss_energy /
+                                 gpss_mass return them while the field and the
+                                 parameters are unchanged -- so solve!'s energy
+                                 then timeStep! (NumModels.jl:33-35) costs no
+                                 read-only passes */
 
 /* split schemes of gpss_step */
 #define GPSS_LIE 1            /* NumModelSplit1: L(dt) N(dt) */

@@ -33,8 +33,8 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_NOMASSLOCK, GPSS_FLAG_NOMERGE,
-                   GPSS_FLAG_PIPE, GPSS_FLAG_PLAIN)
+from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_ENERGY_CACHE, GPSS_FLAG_NOMASSLOCK,
+                   GPSS_FLAG_NOMERGE, GPSS_FLAG_PIPE, GPSS_FLAG_PLAIN)
 
 __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "PotentialZero",
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
@@ -207,7 +207,7 @@ class _SplitModel:
 
     def __init__(self, f: Field, param: GrossPitaevskiiParameters, dt, niter, freqbckp, *,
                  precision="fp64", form="fused", merge=True, masslock=True, pipeline=False,
-                 writers=()):
+                 energy_cache=False, writers=()):
         if f._owner is not None:
             raise ValueError("this field already belongs to a model")
         if form not in ("fused", "plain"):
@@ -228,7 +228,8 @@ class _SplitModel:
         lo = (ctypes.c_double * 3)(*(list(g.min) + [0.0] * (3 - nd)))
         hi = (ctypes.c_double * 3)(*(list(g.max) + [1.0] * (3 - nd)))
         flags = ((GPSS_FLAG_PLAIN if form == "plain" else 0) | (0 if merge else GPSS_FLAG_NOMERGE)
-                 | (0 if masslock else GPSS_FLAG_NOMASSLOCK) | (GPSS_FLAG_PIPE if pipeline else 0))
+                 | (0 if masslock else GPSS_FLAG_NOMASSLOCK) | (GPSS_FLAG_PIPE if pipeline else 0)
+                 | (GPSS_FLAG_ENERGY_CACHE if energy_cache else 0))
         h = ctypes.c_void_p()
         _lib.check(L.gpss_create(ctypes.byref(h), nd, n, lo, hi, _PRECISION[precision], flags))
         self._h = h
@@ -509,7 +510,9 @@ def chemical_potential(n: _SplitModel) -> float:
 def solve(n: _SplitModel, istart: int = 1):
     """solve!(n; istart) (NumModels.jl:23-46): energy then timeStep! every
     iteration, writers every freqbckp iterations.  Writers are callables
-    ``w(field, prefix, istep, dt)``."""
+    ``w(field, prefix, istep, dt)``.  A model made with ``energy_cache=True``
+    (real time, Omega = 0, fused) measures the energies inside each step's
+    last passes, so the energy call of the next iteration launches nothing."""
     res = []
     nkt = 0
     for w in n.writers:

@@ -27,6 +27,7 @@ GPSS_FLAG_PLAIN = 1
 GPSS_FLAG_NOMERGE = 2
 GPSS_FLAG_NOMASSLOCK = 4
 GPSS_FLAG_PIPE = 8
+GPSS_FLAG_ENERGY_CACHE = 16
 GPSS_LIE = 1
 GPSS_STRANG = 2
 

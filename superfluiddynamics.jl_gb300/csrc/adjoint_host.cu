@@ -253,6 +253,7 @@ int gpss_adjoint(gpss_ctx *c, const double *psi_target, int nsteps, int K, doubl
 {
     NvtxRange nvtx_("gpss_adjoint");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!psi_target || !loss) return fail(c, GPSS_EINVAL, "gpss_adjoint: null psi_target or loss");
     if (nsteps < 1 || K < 1) return fail(c, GPSS_EINVAL, "gpss_adjoint: need nsteps >= 1 and K >= 1");
     if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "dt must be finite");

@@ -40,6 +40,10 @@ struct gpss_ctx {
     double cD = -0.5, beta = 1.0, omega = 0.0;
     bool have_psi = false;
     bool have_V = false;
+    // energies of the field as of `version` (GPSS_FLAG_ENERGY_CACHE); every
+    // entry point that may change the field or the parameters bumps version
+    uint64_t version = 0, ecache_version = ~uint64_t(0);
+    double ecache[5] = {0, 0, 0, 0, 0}, ecache_mass = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
     void *psi = nullptr;      // device field (float2 or double2)

@@ -306,7 +306,7 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if (ndim != 2 && ndim != 3) return fail(nullptr, GPSS_EINVAL, "ndim must be 2 or 3 (got %d)", ndim);
     if (precision != GPSS_FP64 && precision != GPSS_FP32)
         return fail(nullptr, GPSS_EINVAL, "precision must be GPSS_FP64 or GPSS_FP32 (got %d)", precision);
-    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_PIPE))
+    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_PIPE | GPSS_FLAG_ENERGY_CACHE))
         return fail(nullptr, GPSS_EINVAL, "unknown flags 0x%x", flags);
     for (int a = 0; a < ndim; a++) {
         if (!is_pow2(n[a]) || n[a] < 2 || n[a] > 256)
@@ -389,6 +389,7 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
 int gpss_set_params(gpss_ctx *c, double coeffD, double beta, double omega)
 {
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!std::isfinite(coeffD) || !std::isfinite(beta) || !std::isfinite(omega))
         return fail(c, GPSS_EINVAL, "parameters must be finite");
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -403,6 +404,7 @@ int gpss_set_params(gpss_ctx *c, double coeffD, double beta, double omega)
 int gpss_set_potential(gpss_ctx *c, const double *V)
 {
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     CUDA_TRY(c, cudaSetDevice(c->device));
     clear_graphs(c);
     if (!V) { c->have_V = false; return GPSS_OK; }
@@ -424,6 +426,7 @@ int gpss_upload(gpss_ctx *c, const double *psi)
 {
     NvtxRange nvtx_("gpss_upload");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!psi) return fail(c, GPSS_EINVAL, "gpss_upload: null psi");
     CUDA_TRY(c, cudaSetDevice(c->device));
     if (c->precision == GPSS_FP64) {
@@ -460,14 +463,34 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
 {
     NvtxRange nvtx_("gpss_step");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (nsteps < 0) return fail(c, GPSS_EINVAL, "nsteps must be >= 0");
     if (scheme != GPSS_LIE && scheme != GPSS_STRANG) return fail(c, GPSS_EINVAL, "scheme must be 1 (Lie) or 2 (Strang)");
     if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "dt must be finite");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
     if (nsteps == 0 && !diag) return GPSS_OK;
-    if (c->precision == GPSS_FP32) return step_impl<float>(c, nsteps, scheme, imag, dt, diag);
-    return step_impl<double>(c, nsteps, scheme, imag, dt, diag);
+    // GPSS_FLAG_ENERGY_CACHE: where the final passes can measure the energies
+    // at no extra sweep (merged real-time Strang), do so and keep them
+    gpss_diag own;
+    gpss_diag *d = diag;
+    if (!d && (c->flags & GPSS_FLAG_ENERGY_CACHE) && !imag && scheme == GPSS_STRANG && c->omega == 0.0 &&
+        !(c->flags & (GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE)) && nsteps > 0)
+        d = &own;
+    const int rc = c->precision == GPSS_FP32 ? step_impl<float>(c, nsteps, scheme, imag, dt, d)
+                                             : step_impl<double>(c, nsteps, scheme, imag, dt, d);
+    if (rc == GPSS_OK && d) {
+        for (int i = 0; i < 5; i++) c->ecache[i] = d->energy[i];
+        c->ecache_mass = d->mass;
+        c->ecache_version = c->version;
+    }
+    return rc;
+}
+
+// the cached energies of the current field (GPSS_FLAG_ENERGY_CACHE), if any
+static bool ecache_fresh(const gpss_ctx *c)
+{
+    return (c->flags & GPSS_FLAG_ENERGY_CACHE) && c->ecache_version == c->version;
 }
 
 
@@ -477,6 +500,10 @@ int gpss_energy(gpss_ctx *c, double *out)
     NvtxRange nvtx_("gpss_energy");
     if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_energy: null out") : GPSS_EINVAL;
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    if (ecache_fresh(c)) {
+        for (int i = 0; i < 5; i++) out[i] = c->ecache[i];
+        return GPSS_OK;
+    }
     CUDA_TRY(c, cudaSetDevice(c->device));
     if (c->precision == GPSS_FP32) return energy_impl<float>(c, out, nullptr);
     return energy_impl<double>(c, out, nullptr);
@@ -501,6 +528,10 @@ static int raw_mass(gpss_ctx *c, double *out)
 int gpss_mass(gpss_ctx *c, double *out)
 {
     if (!c || !out) return c ? fail(c, GPSS_EINVAL, "gpss_mass: null out") : GPSS_EINVAL;
+    if (c->have_psi && ecache_fresh(c)) {
+        *out = c->ecache_mass;
+        return GPSS_OK;
+    }
     double raw;
     GPSS_TRY(raw_mass(c, &raw));
     *out = times_cell(c, raw);
@@ -521,6 +552,7 @@ int gpss_normalize(gpss_ctx *c)
 {
     NvtxRange nvtx_("gpss_normalize");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
     return c->precision == GPSS_FP32 ? normalize_impl<float>(c) : normalize_impl<double>(c);
@@ -531,6 +563,7 @@ int gpss_ground_state(gpss_ctx *c, double dt, double tol, int64_t max_steps, int
 {
     NvtxRange nvtx_("gpss_ground_state");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!(dt > 0) || !(tol > 0) || max_steps < 1 || check_every < 1)
         return fail(c, GPSS_EINVAL, "ground_state: need dt > 0, tol > 0, max_steps >= 1, check_every >= 1");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
@@ -604,6 +637,7 @@ int64_t gpss_device_bytes(const gpss_ctx *c)
 int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double *ms_per_launch)
 {
     if (!c || !ms_per_launch) return c ? fail(c, GPSS_EINVAL, "null argument") : GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (axis < 0 || axis >= c->ndim || reps < 1 || (mode != 0 && mode != 1))
         return fail(c, GPSS_EINVAL, "time_pass: bad axis/mode/reps");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");

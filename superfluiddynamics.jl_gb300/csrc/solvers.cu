@@ -296,6 +296,7 @@ int gpss_rk_step(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
 {
     NvtxRange nvtx_("gpss_rk_step");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "gpss_rk_step: no field uploaded");
     if (nsteps < 0) return fail(c, GPSS_EINVAL, "gpss_rk_step: nsteps < 0");
     if (stepper != 1 && stepper != 2 && stepper != 4)
@@ -312,6 +313,7 @@ int gpss_implicit_step(gpss_ctx *c, int nsteps, int scheme, double dt, int nkryl
 {
     NvtxRange nvtx_("gpss_implicit_step");
     if (!c) return GPSS_EINVAL;
+    c->version++;  // the field or the parameters may change
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "gpss_implicit_step: no field uploaded");
     if (nsteps < 0 || nkrylov < 1 || nnewton < 1)
         return fail(c, GPSS_EINVAL, "gpss_implicit_step: need nsteps >= 0, nkrylov >= 1, nnewton >= 1");

@@ -469,3 +469,49 @@ def test_fullsize_time_reversal_fp32(sfd, O, W):
     assert O.rel_l2(mid, c["psi"]) > 1e-2          # the field did move
     assert O.rel_l2(back, c["psi"]) < 1e-5
     assert abs(e1[3] - e0[3]) < 1e-5 * abs(e0[3])
+
+
+# ----------------------------------------------------------- energy cache --
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_energy_cache_solve(sfd, O, precision):
+    """GPSS_FLAG_ENERGY_CACHE: solve!'s energy-then-timeStep! sequence gives
+    the same energy records as without the cache, with 3 instead of 9 passes
+    per iteration beyond the step; the cache follows every change of the
+    field and of the parameters."""
+    shape, bounds = (32, 16, 8), ((-5.0, 5.0), (-4.0, 4.0), (-3.0, 3.0))
+    psi0 = random_field(shape, seed=5)
+    V = O.quadratic_potential(shape, bounds)
+    L = sfd._lib.lib()
+    res, launches = {}, {}
+    for cache in (False, True):
+        g = sfd.Grid(shape, bounds)
+        f = sfd.Field(g)
+        f.phi = psi0
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=-0.5, beta=30.0)
+        n = sfd.NumModelSplit2(f, p, 2e-3, 20, 100, precision=precision, energy_cache=cache)
+        l0 = L.gpss_launch_count(n.handle)
+        res[cache] = np.array(sfd.solve(n))
+        launches[cache] = L.gpss_launch_count(n.handle) - l0
+        if cache:
+            # a new field, then new parameters: the energies follow
+            n.f.phi = psi0
+            n.upload()
+            f2 = sfd.Field(sfd.Grid(shape, bounds))
+            f2.phi = psi0
+            fresh = sfd.NumModelSplit2(f2, p, 2e-3, 1, 1, precision=precision)
+            assert np.allclose(n.energies(), fresh.energies(), rtol=1e-12, atol=0)
+            p2 = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=-0.5, beta=10.0)
+            n.step(3)
+            n.set_params(p2)
+            fresh.set_params(p2)
+            fresh.step(3)  # the same 3 steps, now under the new parameters
+            n.f.phi = psi0
+            n.upload()
+            n.step(3)
+            assert np.allclose(n.energies(), fresh.energies(), rtol=1e-12 if precision == "fp64" else 1e-6, atol=0)
+            fresh.close()
+        n.close()
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    scale = np.max(np.abs(res[False][:, 2:]))
+    assert np.max(np.abs(res[True] - res[False])) <= tol * scale
+    assert launches[True] < launches[False]
