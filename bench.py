@@ -69,6 +69,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the accuracy, cfg2, cfg4 and cuFFT measurements")
+    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve"], default=None,
+                    help="run one secondary measurement alone and print it (profiling runs)")
+    ap.add_argument("--only-steps", type=int, default=None,
+                    help="with --only imag/solve: time steps (iterations) to time")
     return ap.parse_args()
 
 
@@ -360,6 +364,48 @@ def measure_rk(sfd, c, L, steps=4):
     return out
 
 
+def measure_solve(sfd, c, iters=20):
+    """solve! (energy then timeStep! every iteration, NumModels.jl:23-46) on the
+    cfg1 field at 256^3, FP32, with and without GPSS_FLAG_ENERGY_CACHE."""
+    out = {"workload": f"cfg1 field, 256^3, FP32, solve! with {iters} iterations (energy + one Strang step each)"}
+    for cache in (False, True):
+        grid = sfd.Grid(c["shape"], c["bounds"])
+        f = sfd.Field(grid)
+        f.phi = c["psi"]
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+        m = sfd.NumModelSplit2(f, p, c["dt"], 2, 1000, precision="fp32", energy_cache=cache)
+        sfd.solve(m)  # warm-up (3 iterations)
+        m.niter = iters - 1
+        t0 = time.perf_counter()
+        sfd.solve(m)
+        t = time.perf_counter() - t0
+        m.close(download=False)
+        out["cache" if cache else "no_cache"] = {"ms_per_iteration": t / iters * 1e3}
+    return out
+
+
+def run_only(args):
+    """One secondary measurement alone (for profiling it), one JSON line."""
+    import importlib
+    import __graft_entry__ as g
+    sfd = g.load_package()
+    from sfd_gb300 import _lib
+    W = importlib.import_module("sfd_gb300.workloads")
+    L = _lib.lib()
+    if args.only == "imag":
+        r = measure_imag(sfd, W, L, steps=args.only_steps or 200)
+    elif args.only == "adjoint":
+        r = measure_adjoint(sfd, W)
+    elif args.only == "batch":
+        r = measure_batch(sfd, W)
+    elif args.only == "rk4":
+        r = measure_rk(sfd, W.cfg1(256), L)
+    else:
+        r = measure_solve(sfd, W.cfg1(256), iters=args.only_steps or 20)
+    print(json.dumps(r), flush=True)
+    return 0
+
+
 def measure_cufft(c, n, reps=20):
     """The same directional pass (FFT -> phase multiply -> inverse FFT) through
     cuFFT (torch.fft, complex64) on the 256^3 field, per axis, for comparison."""
@@ -531,6 +577,7 @@ def run_gpss(args, rank, world, local):
         extra["imag_time"] = measure_imag(sfd, W, L)
         extra["adjoint"] = measure_adjoint(sfd, W)
         extra["rk4"] = measure_rk(sfd, c, L)
+        extra["solve"] = measure_solve(sfd, c)
         cu = measure_cufft(c, args.n)
         if cu:
             cu["gpss_pass_ms"] = per_axis
@@ -589,6 +636,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.only:
+        return run_only(args)
     return run_gpss(args, rank, world, local)
 
 
