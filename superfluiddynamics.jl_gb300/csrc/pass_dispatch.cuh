@@ -62,21 +62,25 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
     switch (mode) {
     case MODE_FUSED: {
         // the leanest instantiation that does everything the arguments ask for
-        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr ||
-                          a.pre_out != nullptr || a.adj_pre != nullptr;
+        const bool adj = a.pre_out != nullptr || a.adj_pre != nullptr;
+        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr;
         const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
         if (a.nl_pre || a.dot_with) {
-            if (diag || a.nl_mode != NL_NONE) return cudaErrorInvalidValue;
+            if (diag || adj || a.nl_mode != NL_NONE) return cudaErrorInvalidValue;
             return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_IMAGM>(a, blocks, s);
         }
         if constexpr (sizeof(T) == 4 && N >= 64) {
             if (a.plane_nl || a.plane_scale) {
-                if (diag) return cudaErrorInvalidValue;  // planes carry no energy sums or rotation
+                if (diag || adj) return cudaErrorInvalidValue;  // planes carry no energy sums, rotation or adjoint
                 if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_PLANE | FEAT_NL>(a, blocks, s);
                 return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_PLANE>(a, blocks, s);
             }
         }
         if (diag) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
+        if (adj) {
+            if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ | FEAT_NL>(a, blocks, s);
+            return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ>(a, blocks, s);
+        }
         if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NL>(a, blocks, s);
         return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NONE>(a, blocks, s);
     }
@@ -127,7 +131,22 @@ template <typename T, int N> static int lines_per_cta_n(bool xl)
     return xl ? PassShape<T, N, true>::W : PassShape<T, N, false>::W;
 }
 
+// The instantiations for n = 64, 128 and 256 (the large ones) live in their
+// own translation units (pass_<prec>_<n>.cu), compiled in parallel.
+#define GPSS_DECLARE_PASS_N(T, SUFFIX, N)                                                      \
+    cudaError_t launch_pass_##SUFFIX##_##N(int mode, bool xl, const PassArgs<T> &a, int blocks, \
+                                           cudaStream_t s);
+#define GPSS_DEFINE_PASS_N(T, SUFFIX, N)                                                       \
+    cudaError_t launch_pass_##SUFFIX##_##N(int mode, bool xl, const PassArgs<T> &a, int blocks, \
+                                           cudaStream_t s)                                     \
+    {                                                                                          \
+        return launch_pass_n<T, N>(mode, xl, a, blocks, s);                                    \
+    }
+
 #define GPSS_DEFINE_PASS_DISPATCH(T, SUFFIX)                                                   \
+    GPSS_DECLARE_PASS_N(T, SUFFIX, 64)                                                         \
+    GPSS_DECLARE_PASS_N(T, SUFFIX, 128)                                                        \
+    GPSS_DECLARE_PASS_N(T, SUFFIX, 256)                                                        \
     cudaError_t launch_pipe_##SUFFIX(bool xl, int n, const PassArgs<T> &a, int ntiles,         \
                                      cudaStream_t s)                                           \
     {                                                                                          \
@@ -150,9 +169,9 @@ template <typename T, int N> static int lines_per_cta_n(bool xl)
         case 8: return launch_pass_n<T, 8>(mode, xl, a, blocks, s);                            \
         case 16: return launch_pass_n<T, 16>(mode, xl, a, blocks, s);                          \
         case 32: return launch_pass_n<T, 32>(mode, xl, a, blocks, s);                          \
-        case 64: return launch_pass_n<T, 64>(mode, xl, a, blocks, s);                          \
-        case 128: return launch_pass_n<T, 128>(mode, xl, a, blocks, s);                        \
-        case 256: return launch_pass_n<T, 256>(mode, xl, a, blocks, s);                        \
+        case 64: return launch_pass_##SUFFIX##_64(mode, xl, a, blocks, s);                     \
+        case 128: return launch_pass_##SUFFIX##_128(mode, xl, a, blocks, s);                   \
+        case 256: return launch_pass_##SUFFIX##_256(mode, xl, a, blocks, s);                   \
         default: return cudaErrorInvalidValue;                                                 \
         }                                                                                      \
     }                                                                                          \

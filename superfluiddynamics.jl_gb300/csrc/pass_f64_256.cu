@@ -1,0 +1,5 @@
+// FP64 instantiations of the directional pass kernels for lines of 256 cells.
+#include "pass_dispatch.cuh"
+namespace gpss {
+GPSS_DEFINE_PASS_N(double, f64, 256)
+}

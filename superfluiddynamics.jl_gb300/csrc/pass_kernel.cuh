@@ -78,7 +78,9 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //              prologue of the first pass (nl_pre, after the deferred
 //              factor, its result also stored to nl_pre_out) and the mass sum
 //              of the last pass replaced by Re sum conj(dot_with) psi
-enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8 };
+//   FEAT_ADJ   the discrete adjoint's epilogues (pre_out, adj_pre) without
+//              the energy sums (FEAT_DIAG includes them as well)
+enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -332,6 +334,7 @@ pass_kernel(const PassArgs<T> a)
     constexpr bool kNL = (FEAT & FEAT_NL) != 0, kDiag = (FEAT & FEAT_DIAG) != 0;
     constexpr bool kPlane = (FEAT & FEAT_PLANE) != 0 && sizeof(T) == 4;
     constexpr bool kImagM = (FEAT & FEAT_IMAGM) != 0;
+    constexpr bool kAdj = kDiag || (FEAT & FEAT_ADJ) != 0;
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -587,7 +590,7 @@ pass_kernel(const PassArgs<T> a)
 
     // ---- epilogue: positions r + N2 j
     if constexpr (MODE == MODE_FUSED || MODE == MODE_INV) {
-        if constexpr (MODE == MODE_FUSED && kDiag) {
+        if constexpr (MODE == MODE_FUSED && kAdj) {
             if (a.pre_out && valid) {
 #pragma unroll
                 for (int j = 0; j < N1; j++) a.pre_out[base + (uint32_t)(r + N2 * j) * st] = v[j];
