@@ -209,13 +209,13 @@ int gpss_batch_set_run(gpss_batch *b, int run, double beta, const double *V, con
 int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out);
 int gpss_batch_download(gpss_batch *b, int run, double *psi);
 /* the autotuner's choice (policy 0: runs up to 128^2 in shared memory; 1: up to 64^2),
- * queue order (0: largest first, 1: as given), stacking (1: the 256^2 runs of a box go
- * through the directional pass kernels as one stack of planes) and the trial times in ms
- * (8 entries: index = 4 stack + 2 policy + order; stacked trials only when a box holds
- * two or more 256^2 runs) */
+ * queue order (0: largest first, 1: as given), stacking (the runs of one size and box,
+ * two or more, go through the directional pass kernels as one stack of planes: stack 1
+ * the 256^2 runs, 2 also the 128^2 ones, 3 every size) and the trial times in ms (16
+ * entries: index = 4 stack + 2 policy + order; 1e30 for candidates not tried) */
 int gpss_batch_tuning(const gpss_batch *b, int *policy, int *order, int *stack, float *trial_ms);
-/* fix the launch choice instead of autotuning it (stack = 1 needs a box holding two
- * or more 256^2 runs; otherwise it is ignored) */
+/* fix the launch choice instead of autotuning it (stack 0 to 3; sizes without a stack
+ * stay in the persistent launch) */
 int gpss_batch_set_tuning(gpss_batch *b, int policy, int order, int stack);
 
 /* ---- timing and integration helpers (no reference counterpart) ---- */

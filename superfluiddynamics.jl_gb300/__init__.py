@@ -581,7 +581,7 @@ class BatchSplit2:
 
     def tuning(self):
         pol, order, stack = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        ms = (ctypes.c_float * 8)()
+        ms = (ctypes.c_float * 16)()
         self._ck(_lib.lib().gpss_batch_tuning(self._h, ctypes.byref(pol), ctypes.byref(order), ctypes.byref(stack),
                                               ms))
         return {"policy": pol.value, "order": order.value, "stack": stack.value, "trial_ms": list(ms)}

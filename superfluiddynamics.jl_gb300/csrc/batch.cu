@@ -379,6 +379,7 @@ __global__ void k_plane_finish(const double *__restrict__ partials, int chunks, 
 // 256^2 runs of one box integrated as a stack of planes (see the file comment)
 struct BatchStack {
     int set = 0, n = 0, count = 0;
+    int level = 1;                   // stacked from stack mode `level` up: 1 (256^2), 2 (128^2), 3 (64^2)
     int64_t off = 0;                 // element offset of plane 0 (the planes are consecutive)
     std::vector<int> runs;           // run index of each plane
     int *d_plane_run = nullptr;
@@ -411,14 +412,14 @@ struct gpss_batch {
     double tables_dt = NAN;
     int64_t total = 0;
     int policy = -1, order_mode = 0;  // tuned
-    float tuned_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float tuned_ms[16] = {};          // trial time per candidate: 4 stack + 2 policy + order
     cudaGraphExec_t graph = nullptr;
     int graph_nsteps = -1;
     double graph_dt = NAN;
     std::vector<BatchStack> stacks;
     std::vector<TableSet> h_sets;     // host copy of the device table pointers
-    int stack_mode = 0;               // tuned: 1 = stackable runs go through the pass kernels
-    int nqueue[2] = {0, 0};           // queue lengths without / with stacking
+    int stack_mode = 0;               // tuned: the stacks of level <= stack_mode go through the pass kernels
+    int nqueue[4] = {0, 0, 0, 0};     // queue length per stack mode
     std::string err;
 };
 
@@ -600,10 +601,11 @@ static PassArgs<float> stack_args(const BatchStack &st, int axis, float2 *psi, c
 
 // The stacked runs: the persistent kernel's merged Strang sequence and FP32
 // mass lock, with the x and y passes of every plane in one launch each.
-static cudaError_t run_stacks(gpss_batch *b, int nsteps, double dt, double *mass_out)
+static cudaError_t run_stacks(gpss_batch *b, int nsteps, double dt, double *mass_out, int mode)
 {
     (void)dt;
     for (auto &st : b->stacks) {
+        if (st.level > mode) continue;
         const TableSet &ts = b->h_sets[(size_t)st.set];
         const int n = st.n, P = st.count;
         const int64_t cells = (int64_t)n * n;
@@ -651,10 +653,11 @@ static cudaError_t run_batch(gpss_batch *b, int policy, int order_mode, int stac
 {
     cudaError_t e = launch_policy(b, policy, make_args(b, nsteps, dt, order_mode, stack_mode));
     if (e != cudaSuccess || !stack_mode) return e;
-    return run_stacks(b, nsteps, dt, b->d_mass);
+    return run_stacks(b, nsteps, dt, b->d_mass, stack_mode);
 }
 
-// queue: d_order holds 4 lists of nruns: [stack][order] (stack 1 lists leave the stacked runs out)
+// queue: d_order holds 8 lists of nruns: [stack mode][order] (the lists of stack mode m leave out
+// the runs of the stacks of level <= m)
 static BatchArgs make_args(gpss_batch *b, int nsteps, double dt, int order_mode, int stack_mode)
 {
     BatchArgs A;
@@ -716,13 +719,15 @@ int gpss_batch_create(gpss_batch **out, int nruns, const int64_t *n, const doubl
             st.runs.push_back(r);
         }
         st.count = (int)st.runs.size();
-        if (st.n == 256 && st.count >= 2) b->stacks.push_back(st);
+        st.level = st.n == 256 ? 1 : (st.n == 128 ? 2 : 3);
+        if (st.count >= 2) b->stacks.push_back(st);
     }
     b->total = off;
-    auto stacked = [&](int r) {
+    auto stacked = [&](int r, int mode) {
         for (const auto &st : b->stacks)
-            for (int q : st.runs)
-                if (q == r) return true;
+            if (st.level <= mode)
+                for (int q : st.runs)
+                    if (q == r) return true;
         return false;
     };
     b->order_given.resize((size_t)nruns);
@@ -735,21 +740,22 @@ int gpss_batch_create(gpss_batch **out, int nruns, const int64_t *n, const doubl
     if (cudaMalloc(&b->d_psi, (size_t)off * sizeof(float2)) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_V, (size_t)off * sizeof(float)) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_runs, (size_t)nruns * sizeof(BatchRun)) != cudaSuccess) return bail(GPSS_ENOMEM);
-    if (cudaMalloc(&b->d_order, (size_t)nruns * 4 * sizeof(int)) != cudaSuccess) return bail(GPSS_ENOMEM);
+    if (cudaMalloc(&b->d_order, (size_t)nruns * 8 * sizeof(int)) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_mass, (size_t)nruns * sizeof(double)) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_queue, sizeof(int) * 2) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_status, sizeof(int) * 2) != cudaSuccess) return bail(GPSS_ENOMEM);
     std::vector<int> orders(b->order_big);
     orders.insert(orders.end(), b->order_given.begin(), b->order_given.end());
     b->nqueue[0] = nruns;
-    for (const auto *src : {&b->order_big, &b->order_given}) {
-        std::vector<int> kept;
-        for (int r : *src)
-            if (!stacked(r)) kept.push_back(r);
-        b->nqueue[1] = (int)kept.size();
-        kept.resize((size_t)nruns, 0);
-        orders.insert(orders.end(), kept.begin(), kept.end());
-    }
+    for (int mode = 1; mode <= 3; mode++)
+        for (const auto *src : {&b->order_big, &b->order_given}) {
+            std::vector<int> kept;
+            for (int r : *src)
+                if (!stacked(r, mode)) kept.push_back(r);
+            b->nqueue[mode] = (int)kept.size();
+            kept.resize((size_t)nruns, 0);
+            orders.insert(orders.end(), kept.begin(), kept.end());
+        }
     if (cudaMemcpy(b->d_order, orders.data(), orders.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(GPSS_ECUDA);
     for (auto &st : b->stacks) {
@@ -850,9 +856,13 @@ int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out)
         cudaEventCreate(&e1);
         const int trial = std::min(nsteps, 16);
         float best = 1e30f;
-        const int ncand = b->stacks.empty() ? 4 : 8;
-        for (int cand = 0; cand < ncand; cand++) {
+        bool has_level[4] = {true, false, false, false};
+        for (const auto &st : b->stacks) has_level[st.level] = true;
+        for (int cand = 0; cand < 16; cand++) {
             const int policy = (cand >> 1) & 1, order = cand & 1, stack = cand >> 2;
+            b->tuned_ms[cand] = 1e30f;
+            // stack modes that stack nothing new, and launch choices without a queue, are not tried
+            if (!has_level[stack] || (b->nqueue[stack] == 0 && (policy || order))) continue;
             cudaError_t e = run_batch(b, policy, order, stack, trial, dt);  // warm-up
             float ms = 1e30f;
             for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {  // the faster of two timed trials
@@ -919,11 +929,11 @@ int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out)
 int gpss_batch_set_tuning(gpss_batch *b, int policy, int order, int stack)
 {
     if (!b) return GPSS_EINVAL;
-    if (policy < 0 || policy > 1 || order < 0 || order > 1 || stack < 0 || stack > 1)
-        return bfail(b, GPSS_EINVAL, "gpss_batch_set_tuning: policy, order and stack are 0 or 1");
+    if (policy < 0 || policy > 1 || order < 0 || order > 1 || stack < 0 || stack > 3)
+        return bfail(b, GPSS_EINVAL, "gpss_batch_set_tuning: policy and order are 0 or 1, stack 0 to 3");
     b->policy = policy;
     b->order_mode = order;
-    b->stack_mode = b->stacks.empty() ? 0 : stack;
+    b->stack_mode = stack;
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -938,7 +948,7 @@ int gpss_batch_tuning(const gpss_batch *b, int *policy, int *order, int *stack, 
     if (order) *order = b->order_mode;
     if (stack) *stack = b->stack_mode;
     if (trial_ms)
-        for (int i = 0; i < 8; i++) trial_ms[i] = b->tuned_ms[i];
+        for (int i = 0; i < 16; i++) trial_ms[i] = b->tuned_ms[i];
     return GPSS_OK;
 }
 

@@ -13,8 +13,10 @@ def _lib(built_lib):
     return built_lib
 
 
-@pytest.mark.parametrize("tuning", [None, (0, 0, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1)],
-                         ids=["autotuned", "p0", "p1", "p0-stacked", "p1-stacked"])
+@pytest.mark.parametrize("tuning", [None, (0, 0, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1), (0, 0, 2), (1, 1, 2),
+                                    (0, 0, 3)],
+                         ids=["autotuned", "p0", "p1", "p0-stacked", "p1-stacked", "p0-stacked128",
+                              "p1-stacked128", "all-stacked"])
 def test_batch_matches_single_runs_and_oracle(sfd, O, W, tuning):
     """Every launch choice: the persistent kernel's policies, and the 256^2
     runs as a stack of planes through the directional pass kernels."""
@@ -27,7 +29,7 @@ def test_batch_matches_single_runs_and_oracle(sfd, O, W, tuning):
         b.set_tuning(*tuning)
     masses = b.step(nsteps, dt)
     tune = b.tuning()
-    assert tune["policy"] in (0, 1) and tune["order"] in (0, 1) and tune["stack"] in (0, 1)
+    assert tune["policy"] in (0, 1) and tune["order"] in (0, 1) and tune["stack"] in (0, 1, 2, 3)
     if tuning is not None:
         assert (tune["policy"], tune["order"], tune["stack"]) == tuning
     for i, r in enumerate(runs):
