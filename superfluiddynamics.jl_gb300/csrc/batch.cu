@@ -396,6 +396,10 @@ struct gpss_batch {
     double coeffD = -0.5;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // the persistent launch runs on side_stream beside the stacked passes
+    // (disjoint runs), forked from and joined back into stream
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::vector<BatchRun> runs;
     std::vector<int> order_big, order_given;
     std::vector<std::pair<int, std::pair<double, double>>> set_keys;  // (n, (Lx, Ly))
@@ -541,7 +545,7 @@ static int build_tables(gpss_batch *b, double dt)
     return GPSS_OK;
 }
 
-static cudaError_t launch_policy(gpss_batch *b, int policy, const BatchArgs &A)
+static cudaError_t launch_policy(gpss_batch *b, int policy, const BatchArgs &A, cudaStream_t stream)
 {
     const size_t smem = policy_smem(policy);
     int nsm = 0, per = 0;
@@ -560,10 +564,10 @@ static cudaError_t launch_policy(gpss_batch *b, int policy, const BatchArgs &A)
     if (per < 1) return cudaErrorInvalidConfiguration;
     if (A.nruns < 1) return cudaSuccess;  // every run is stacked
     int grid = std::min(nsm * per, A.nruns);
-    e = cudaMemsetAsync(A.queue, 0, sizeof(int), b->stream);
+    e = cudaMemsetAsync(A.queue, 0, sizeof(int), stream);
     if (e != cudaSuccess) return e;
-    if (policy == 0) launch_pdl(batch_kernel<0>, dim3(grid), dim3(kThreads), smem, b->stream, A);
-    else launch_pdl(batch_kernel<1>, dim3(grid), dim3(kThreads), smem, b->stream, A);
+    if (policy == 0) launch_pdl(batch_kernel<0>, dim3(grid), dim3(kThreads), smem, stream, A);
+    else launch_pdl(batch_kernel<1>, dim3(grid), dim3(kThreads), smem, stream, A);
     return cudaGetLastError();
 }
 
@@ -648,12 +652,23 @@ static cudaError_t run_stacks(gpss_batch *b, int nsteps, double dt, double *mass
 
 static BatchArgs make_args(gpss_batch *b, int nsteps, double dt, int order_mode, int stack_mode);
 
-// one batch integration: the persistent launch over the queued runs, then the stacks
+// one batch integration: the persistent launch over the queued runs and the
+// stacks.  With both, the persistent launch runs on the side stream beside the
+// stacked passes (they touch disjoint runs; the queue kernel's CTAs wait on
+// nothing), forked from and joined back into the batch stream.
 static cudaError_t run_batch(gpss_batch *b, int policy, int order_mode, int stack_mode, int nsteps, double dt)
 {
-    cudaError_t e = launch_policy(b, policy, make_args(b, nsteps, dt, order_mode, stack_mode));
-    if (e != cudaSuccess || !stack_mode) return e;
-    return run_stacks(b, nsteps, dt, b->d_mass, stack_mode);
+    const BatchArgs A = make_args(b, nsteps, dt, order_mode, stack_mode);
+    if (!stack_mode) return launch_policy(b, policy, A, b->stream);
+    if (A.nruns < 1) return run_stacks(b, nsteps, dt, b->d_mass, stack_mode);
+    cudaError_t e = cudaEventRecord(b->fork_ev, b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side_stream, b->fork_ev, 0);
+    if (e == cudaSuccess) e = launch_policy(b, policy, A, b->side_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->join_ev, b->side_stream);
+    const cudaError_t es = e == cudaSuccess ? run_stacks(b, nsteps, dt, b->d_mass, stack_mode) : e;
+    // join even after a failure, so that a capture ends with every branch joined
+    const cudaError_t ej = cudaStreamWaitEvent(b->stream, b->join_ev, 0);
+    return es != cudaSuccess ? es : ej;
 }
 
 // queue: d_order holds 8 lists of nruns: [stack mode][order] (the lists of stack mode m leave out
@@ -737,6 +752,9 @@ int gpss_batch_create(gpss_batch **out, int nruns, const int64_t *n, const doubl
                      [&](int x, int y) { return b->runs[(size_t)x].n > b->runs[(size_t)y].n; });
     if (cudaGetDevice(&b->device) != cudaSuccess) return bail(GPSS_ECUDA);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(GPSS_ECUDA);
+    if (cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(GPSS_ECUDA);
+    if (cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(GPSS_ECUDA);
+    if (cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming) != cudaSuccess) return bail(GPSS_ECUDA);
     if (cudaMalloc(&b->d_psi, (size_t)off * sizeof(float2)) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_V, (size_t)off * sizeof(float)) != cudaSuccess) return bail(GPSS_ENOMEM);
     if (cudaMalloc(&b->d_runs, (size_t)nruns * sizeof(BatchRun)) != cudaSuccess) return bail(GPSS_ENOMEM);
@@ -788,6 +806,10 @@ void gpss_batch_destroy(gpss_batch *b)
         for (void *p : sp)
             if (p) cudaFree(p);
     }
+    if (b->side_stream) cudaStreamSynchronize(b->side_stream);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->join_ev) cudaEventDestroy(b->join_ev);
+    if (b->side_stream) cudaStreamDestroy(b->side_stream);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
