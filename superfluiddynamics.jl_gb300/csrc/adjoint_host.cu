@@ -74,7 +74,10 @@ static int adj_group(gpss_ctx *c, void *buf, double dtl, bool reverse, bool nl, 
 //   dL/dpsi0 = L^H(h) g
 // one group per step with N^H fused into its last pass.  Segments of K steps
 // are recomputed from their checkpoint into K state buffers (the same
-// kernels as the forward, so the states are bitwise the forward's).
+// kernels as the forward, so the states are bitwise the forward's).  The
+// recompute of segment s-1 runs on a second stream while the backward sweep
+// works through segment s (two sets of state buffers, alternating): a 256^2
+// pass fills a few dozen SMs, so the two chains share the GPU.
 template <typename T>
 static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int K, double dt, double *loss,
                           double *dLdV, double *dLdpsi0)
@@ -82,9 +85,13 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
     using V = vec2<T>;
     const size_t fb = (size_t)c->total * sizeof(V);
     const int nck = (nsteps + K - 1) / K;
-    // psi0, g, tgt, work, states[K], ckpt[nck]; dv (doubles); reduction scratch
+    // psi0, g, tgt, work, states[2][K], ckpt[nck]; dv (doubles); reduction scratch
     const size_t red_bytes = sizeof(double) * (2 * 152 * 8 + 2);
-    const size_t need = fb * (size_t)(4 + K + nck) + (size_t)c->total * sizeof(double) + red_bytes;
+    const size_t need = fb * (size_t)(4 + 2 * K + nck) + (size_t)c->total * sizeof(double) + red_bytes;
+    if (!c->side) {
+        CUDA_TRY(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        for (auto &e : c->side_ev) CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
     if (c->adj_bytes < need) {
         clear_graphs(c);
         if (c->adj_buf) { cudaStreamSynchronize(c->stream); cudaFree(c->adj_buf); c->adj_buf = nullptr; c->adj_bytes = 0; }
@@ -93,9 +100,9 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
     }
     char *base = static_cast<char *>(c->adj_buf);
     void *psi0 = base, *g = base + fb, *tgt = base + 2 * fb, *work = base + 3 * fb;
-    auto state = [&](int j) { return static_cast<void *>(base + fb * (size_t)(4 + j)); };
-    auto ckpt = [&](int i) { return static_cast<void *>(base + fb * (size_t)(4 + K + i)); };
-    double *dv = reinterpret_cast<double *>(base + fb * (size_t)(4 + K + nck));
+    auto state = [&](int set, int j) { return static_cast<void *>(base + fb * (size_t)(4 + set * K + j)); };
+    auto ckpt = [&](int i) { return static_cast<void *>(base + fb * (size_t)(4 + 2 * K + i)); };
+    double *dv = reinterpret_cast<double *>(base + fb * (size_t)(4 + 2 * K + nck));
     double *red = dv + c->total;
     double *zdev = red + 2 * 152 * 8;
     const double dV = cell_volume(c), h = dt * 0.5;
@@ -120,24 +127,50 @@ static int adjoint_merged(gpss_ctx *c, const double *psi_target, int nsteps, int
         CUDA_TRY(c, launch_overlap<T>((const V *)tgt, (const V *)c->psi, c->total, red, dV, zdev, c->stream));
         CUDA_TRY(c, launch_seed<T>((V *)g, (const V *)tgt, zdev, dV, c->total, c->stream));
         c->launches += 3;
-        // backward, segment by segment from the last
+        // backward, segment by segment from the last; the recomputes run on
+        // the side stream one segment ahead (side_ev: 0 fork, 1 recompute
+        // done, 2 backward through a segment done)
+        cudaStream_t main = c->stream;
+        auto recompute = [&](int seg) -> int {
+            const int start = seg * K, end = std::min(start + K, nsteps);
+            if (end - start < 2) return GPSS_OK;
+            // work = N(pre_start), then pre_{start+j} = L(dt) N(pre_{start+j-1}) into state(j)
+            CUDA_TRY(c, cudaMemcpyAsync(work, ckpt(seg), fb, cudaMemcpyDeviceToDevice, c->stream));
+            cudaError_t e = launch_nl<T>((V *)work, c->have_V ? (const T *)c->V : nullptr, c->beta, dt, 0,
+                                         c->total, c->stream);
+            if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl: %s", cudaGetErrorString(e));
+            c->launches++;
+            for (int j = 1; j < end - start; j++)
+                GPSS_TRY(adj_group<T>(c, work, dt, false, true, dt, state(seg & 1, j), nullptr, nullptr));
+            return GPSS_OK;
+        };
+        auto on_side = [&](auto fn) -> int {  // issue fn's work on the side stream
+            c->stream = c->side;
+            const int rc = fn();
+            c->stream = main;
+            return rc;
+        };
+        CUDA_TRY(c, cudaEventRecord(c->side_ev[0], main));
+        CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->side_ev[0], 0));
+        GPSS_TRY(on_side([&] { return recompute(nck - 1); }));
+        CUDA_TRY(c, cudaEventRecord(c->side_ev[1], c->side));
         for (int seg = nck - 1; seg >= 0; seg--) {
             const int start = seg * K, end = std::min(start + K, nsteps);
-            if (end - start > 1) {
-                // work = N(pre_start), then pre_{start+j} = L(dt) N(pre_{start+j-1}) into state(j)
-                CUDA_TRY(c, cudaMemcpyAsync(work, ckpt(seg), fb, cudaMemcpyDeviceToDevice, c->stream));
-                cudaError_t e = launch_nl<T>((V *)work, c->have_V ? (const T *)c->V : nullptr, c->beta, dt, 0,
-                                             c->total, c->stream);
-                if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "nl: %s", cudaGetErrorString(e));
-                c->launches++;
-                for (int j = 1; j < end - start; j++)
-                    GPSS_TRY(adj_group<T>(c, work, dt, false, true, dt, state(j), nullptr, nullptr));
+            CUDA_TRY(c, cudaStreamWaitEvent(main, c->side_ev[1], 0));  // segment seg recomputed
+            if (seg > 0) {
+                // segment seg-1's states reuse the set of segment seg+1, which
+                // the backward sweep has finished with (side_ev[2])
+                if (seg < nck - 1) CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->side_ev[2], 0));
+                GPSS_TRY(on_side([&] { return recompute(seg - 1); }));
+                CUDA_TRY(c, cudaEventRecord(c->side_ev[1], c->side));
             }
             for (int n = end - 1; n >= start; n--) {
-                const void *pre = n == start ? ckpt(seg) : state(n - start);
+                const void *pre = n == start ? ckpt(seg) : state(seg & 1, n - start);
                 GPSS_TRY(adj_group<T>(c, g, n == nsteps - 1 ? -h : -dt, true, false, dt, nullptr, pre, dv));
             }
+            CUDA_TRY(c, cudaEventRecord(c->side_ev[2], main));
         }
+        CUDA_TRY(c, cudaStreamWaitEvent(main, c->side_ev[1], 0));  // join the side stream
         GPSS_TRY(adj_group<T>(c, g, -h, true, false, 0.0, nullptr, nullptr, nullptr));
         CUDA_TRY(c, cudaMemcpyAsync(c->psi, psi0, fb, cudaMemcpyDeviceToDevice, c->stream));
         return GPSS_OK;

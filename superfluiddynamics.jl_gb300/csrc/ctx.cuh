@@ -66,6 +66,10 @@ struct gpss_ctx {
     // discrete adjoint: buffers kept between calls (sized for adj_nck checkpoints, adj_K states)
     void *adj_buf = nullptr;
     size_t adj_bytes = 0;
+    // the adjoint's second stream (segment recomputes beside the backward
+    // sweep) and its fork/join events, made on first use
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_ev[3] = {nullptr, nullptr, nullptr};
     // CUDA graphs of repeated launch sequences (graph_run), keyed by what they bake in
     struct GraphEntry {
         std::string key;

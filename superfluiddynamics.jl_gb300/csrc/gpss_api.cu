@@ -293,6 +293,12 @@ void gpss_destroy(gpss_ctx *c)
         if (p) cudaFree(p);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : c->side_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
