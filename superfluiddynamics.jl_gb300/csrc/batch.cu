@@ -24,12 +24,14 @@
 //   policy 0  runs up to 128^2 in shared memory (204 KB per CTA, 1 CTA/SM)
 //   policy 1  only runs up to 64^2 in shared memory; 128^2 runs use tiles
 //             (72 KB per CTA, 3 CTAs/SM)
-// the queue order (largest first, or as given), and stacking: the 256^2 runs
-// of one box can instead go through the single-field directional pass kernels
-// as one stack of planes (an n x n x count field whose x and y passes cover
-// every run at once, with per-plane nonlinear constants, potential and FP32
-// mass lock), so that each of them is spread over the whole GPU instead of
-// being one CTA's job; the persistent launch then integrates the other runs.
+// the queue order (largest first, or as given), and stacking: the runs of one
+// size and box can instead go through the single-field directional pass
+// kernels as one stack of planes (an n x n x count field whose x and y passes
+// cover every run at once, with per-plane nonlinear constants, potential and
+// FP32 mass lock), so that each of them is spread over the whole GPU instead
+// of being one CTA's job.  Stack mode 1 stacks the 256^2 runs, 2 also the
+// 128^2 ones, 3 every size; the persistent launch integrates the other runs,
+// on a second stream beside the stacked passes (disjoint runs).
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
