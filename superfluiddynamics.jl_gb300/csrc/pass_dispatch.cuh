@@ -13,10 +13,26 @@ namespace gpss {
 #define GPSS_PASS_WAVES 1
 #endif
 
+// SMs of the current device (cached per device)
+static int sm_count()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 1;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return 1;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 template <typename T, int N, bool XL, int MODE, int FEAT = FEAT_ALL>
 static cudaError_t launch_pass_inst(const PassArgs<T> &a, int tiles, cudaStream_t s)
 {
-    using S = PassShape<T, N, XL>;
+    using S = PassShape<T, N, XL, FEAT>;
+    if (FEAT & FEAT_SMALL) tiles = (a.nlines + S::W - 1) / S::W;  // the host counted default tiles
     auto k = pass_kernel<T, N, XL, MODE, FEAT>;
     static int wave[64] = {0};
     int dev = 0;
@@ -77,6 +93,15 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
             }
         }
         if (diag) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
+        if constexpr (sizeof(T) == 4 && !XL && N >= 64) {
+            // fewer default tiles than SMs: the 128-thread y/z instantiation
+            if (blocks < sm_count()) {
+                if (adj && nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ | FEAT_NL | FEAT_SMALL>(a, blocks, s);
+                if (adj) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ | FEAT_SMALL>(a, blocks, s);
+                if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NL | FEAT_SMALL>(a, blocks, s);
+                return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_SMALL>(a, blocks, s);
+            }
+        }
         if (adj) {
             if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ | FEAT_NL>(a, blocks, s);
             return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ>(a, blocks, s);

@@ -80,7 +80,10 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //              of the last pass replaced by Re sum conj(dot_with) psi
 //   FEAT_ADJ   the discrete adjoint's epilogues (pre_out, adj_pre) without
 //              the energy sums (FEAT_DIAG includes them as well)
-enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16 };
+//   FEAT_SMALL (launch shape, FP32 y/z lines) CTAs of 128 threads, for fields
+//              whose pass would otherwise have fewer tiles than SMs
+enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
+       FEAT_SMALL = 32 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -203,16 +206,20 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #ifndef GPSS_PASS_THREADS_F64
 #define GPSS_PASS_THREADS_F64 64
 #endif
-template <typename T, bool XL> struct PassGeom {
+// Small fields (a 2D y pass of 256 columns is 16 tiles of 16): y/z CTAs of 128
+// threads give twice the tiles (2D 128^2 step 11.4 -> 10.6 us, 256^2 13.1 ->
+// 12.5 us); at 256^3 they would cost the y pass 34 %.
+template <typename T, bool XL, int FEAT = 0> struct PassGeom {
     static constexpr int THREADS =
-        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : GPSS_PASS_THREADS_COL_F32) : GPSS_PASS_THREADS_F64;
+        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : ((FEAT & FEAT_SMALL) ? 128 : GPSS_PASS_THREADS_COL_F32))
+                       : GPSS_PASS_THREADS_F64;
 };
 template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
     static constexpr int SM_THREADS =
-        (MODE == MODE_FUSED && FEAT == FEAT_NONE)
+        (MODE == MODE_FUSED && (FEAT & ~FEAT_SMALL) == FEAT_NONE)
             ? (XL ? GPSS_PASS_SM_THREADS_LEAN_XL_F32 : GPSS_PASS_SM_THREADS_LEAN_F32)
             : GPSS_PASS_SM_THREADS_F32;
-    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? SM_THREADS / PassGeom<T, XL>::THREADS : 1;
+    static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? SM_THREADS / PassGeom<T, XL, FEAT>::THREADS : 1;
 };
 
 template <int N> struct Split {
@@ -220,11 +227,11 @@ template <int N> struct Split {
     static constexpr int N2 = N / N1;
 };
 
-template <typename T, int N, bool XL> struct PassShape {
+template <typename T, int N, bool XL, int FEAT = 0> struct PassShape {
     static constexpr int N1 = Split<N>::N1;
     static constexpr int N2 = Split<N>::N2;
     static constexpr int P = N2;                       // threads per line
-    static constexpr int THREADS = PassGeom<T, XL>::THREADS;
+    static constexpr int THREADS = PassGeom<T, XL, FEAT>::THREADS;
     static constexpr int W = THREADS / P;              // lines per CTA
     static constexpr int LS = N + N1 + N2;             // XL padded line stride (slots)
     static constexpr int DATA = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
@@ -328,7 +335,7 @@ __device__ __forceinline__ void finish_reduction(const PassArgs<T> &a, unsigned 
 }
 
 template <typename T, int N, bool XL, int MODE, int FEAT = FEAT_ALL>
-__global__ void __launch_bounds__(PassGeom<T, XL>::THREADS, PassOcc<T, XL, MODE, FEAT>::MIN_BLOCKS)
+__global__ void __launch_bounds__(PassGeom<T, XL, FEAT>::THREADS, PassOcc<T, XL, MODE, FEAT>::MIN_BLOCKS)
 pass_kernel(const PassArgs<T> a)
 {
     constexpr bool kNL = (FEAT & FEAT_NL) != 0, kDiag = (FEAT & FEAT_DIAG) != 0;
@@ -338,7 +345,7 @@ pass_kernel(const PassArgs<T> a)
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
-    using S = PassShape<T, N, XL>;
+    using S = PassShape<T, N, XL, FEAT>;
     constexpr int N1 = S::N1, N2 = S::N2, P = S::P, W = S::W, LS = S::LS;
     constexpr int THREADS = S::THREADS;
 
