@@ -191,13 +191,16 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #endif
 // the lean FUSED y/z instantiation (FEAT_NONE: kinetic pass only) fits 64
 // registers without spills, so it is compiled for 1024 threads per SM (y pass
-// 69.5 -> 67.2 us at 256^3); the x one spills at 64 (6% slower) but fits 72
-// (896 threads per SM).  The NL instantiation spills at 64 (1% slower).
+// 69.5 -> 67.2 us at 256^3); the x one spills at 64 (6% slower).  With warp
+// barriers and dependent launch the lean x pass runs at 768 threads per SM
+// (80 registers): alone it is 0.6 us slower than at 896, but the 256^3 step
+// is 197.2 -> 195.6 us (the next pass's CTAs find room sooner).  The NL
+// instantiation spills at 64 (1% slower).
 #ifndef GPSS_PASS_SM_THREADS_LEAN_F32
 #define GPSS_PASS_SM_THREADS_LEAN_F32 1024
 #endif
 #ifndef GPSS_PASS_SM_THREADS_LEAN_XL_F32
-#define GPSS_PASS_SM_THREADS_LEAN_XL_F32 896  // 7 CTAs of 128, 72 registers: x 63.8 -> 61.9 us
+#define GPSS_PASS_SM_THREADS_LEAN_XL_F32 768  // 6 CTAs of 128
 #endif
 // FP64: CTAs of 64 threads.  The FP64 kernels are bound by GB300's FP64 rate
 // per SM, so small fields must spread over many SMs (2D 128^2 step 176 -> 88
