@@ -588,7 +588,7 @@ def run_gpss(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         O = oracle_mod()
         v, cores, dt = cpu_sample(c, O, 1, os.cpu_count() or 1)
-        steps = max(1, min(8, int(15.0 / max(dt, 1e-3))))
+        steps = max(1, min(128, int(12.0 / max(dt, 1e-3))))  # about 12 s of CPU work
         if steps > 1:
             v, cores, dt = cpu_sample(c, O, steps, os.cpu_count() or 1)
         cpu = {"value": v / 1e6, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
