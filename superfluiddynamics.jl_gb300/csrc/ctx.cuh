@@ -60,7 +60,7 @@ struct gpss_ctx {
     unsigned int *counter = nullptr;  // arrival counter of the in-kernel reduction finish
     std::vector<PhaseEntry> phases;
     void *rk_buf[4] = {nullptr, nullptr, nullptr, nullptr};  // RK: stage state, lapRot, NL term, sum
-    int *rk_lim = nullptr;    // RK: 2/3-rule limits per inner position (launch_mask_spectrum)
+    int *rk_lim = nullptr;    // RK: 2/3-rule limits per inner position (the FEAT_MASK pass)
     void *im_buf = nullptr;   // implicit schemes: work fields (implicit_impl)
     size_t im_bytes = 0;
     // discrete adjoint: buffers kept between calls (sized for adj_nck checkpoints, adj_K states)

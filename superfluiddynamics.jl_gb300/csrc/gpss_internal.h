@@ -85,9 +85,6 @@ cudaError_t im_mfield(vec2<T> *out, const vec2<T> *M, const vec2<T> *x, int64_t 
 template <typename T>
 cudaError_t launch_nl_term(const vec2<T> *q, const T *V, double beta, vec2<T> *t, int64_t total, cudaStream_t s);
 template <typename T>
-cudaError_t launch_mask_spectrum(vec2<T> *f, const int *lim, int64_t n_last, int64_t inner, int64_t total,
-                                 cudaStream_t s);
-template <typename T>
 cudaError_t launch_rk_combine(const vec2<T> *k, const vec2<T> *t, const vec2<T> *psi0, vec2<T> *acc, vec2<T> *out,
                               int acc_mode, double acc_w, double cf, int from_acc, int64_t total, cudaStream_t s);
 

@@ -81,6 +81,11 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
         const bool adj = a.pre_out != nullptr || a.adj_pre != nullptr;
         const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr;
         const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
+        if (a.mask_lim) {
+            if (diag || adj || nl || a.nl_pre || a.dot_with) return cudaErrorInvalidValue;
+            return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_MASK>(a, blocks, s);
+        }
+        if (!a.phase) return cudaErrorInvalidValue;  // every other fused pass reads a phase table
         if (a.nl_pre || a.dot_with) {
             if (diag || adj || a.nl_mode != NL_NONE) return cudaErrorInvalidValue;
             return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_IMAGM>(a, blocks, s);

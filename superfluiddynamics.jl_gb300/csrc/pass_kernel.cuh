@@ -82,8 +82,11 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //              the energy sums (FEAT_DIAG includes them as well)
 //   FEAT_SMALL (launch shape, FP32 y/z lines) CTAs of 128 threads, for fields
 //              whose pass would otherwise have fewer tiles than SMs
+//   FEAT_MASK  the 2/3 dealiasing filter in place of the phase: on the last
+//              axis of a spectrum already transformed along the others, keep
+//              the modes with |kk| <= mask_lim[line] (scaled by 1/n), zero the rest
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
-       FEAT_SMALL = 32 };
+       FEAT_SMALL = 32, FEAT_MASK = 64 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -164,6 +167,8 @@ template <typename T> struct PassArgs {
     int nl_pre;
     vec2<T> *nl_pre_out;
     const vec2<T> *dot_with;
+    // FEAT_MASK: the largest kept |kk| of each line (-1: none)
+    const int *mask_lim;
 };
 
 // a double-word constant in shared memory: hi and lo adjacent, so one
@@ -345,6 +350,7 @@ pass_kernel(const PassArgs<T> a)
     constexpr bool kPlane = (FEAT & FEAT_PLANE) != 0 && sizeof(T) == 4;
     constexpr bool kImagM = (FEAT & FEAT_IMAGM) != 0;
     constexpr bool kAdj = kDiag || (FEAT & FEAT_ADJ) != 0;
+    constexpr bool kMask = (FEAT & FEAT_MASK) != 0;
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -363,7 +369,7 @@ pass_kernel(const PassArgs<T> a)
     for (int i = tid; i < N; i += THREADS) {
         stw[i] = DWord<V>{a.tw[i], a.tw[N + i]};
         if (S::TWB) stwB[i] = DWord<V>{a.tw[2 * N + i], a.tw[3 * N + i]};
-        if (MODE == MODE_FUSED && prow == 0) sph[i] = DWord<V>{a.phase[i], a.phase[N + i]};
+        if (MODE == MODE_FUSED && !kMask && prow == 0) sph[i] = DWord<V>{a.phase[i], a.phase[N + i]};
     }
 
     const int w = XL ? tid / P : tid % W;
@@ -480,12 +486,21 @@ pass_kernel(const PassArgs<T> a)
                 acc_kin += s2 * (T)(1.0 / N);
                 if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
             }
+            if constexpr (kMask) {
+                const int lim = a.mask_lim[gg];
 #pragma unroll
-            for (int k = 0; k < N1; k++) {
-                const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
-                                          : sph[k];
-                v[k] = cmul2(v[k], p.hi, p.lo);
-                if (tscaled) v[k] = cscale(v[k], tscale);
+                for (int k = 0; k < N1; k++) {
+                    const int kk = k < (N + 1) / 2 ? k : N - k;
+                    v[k] = kk <= lim ? cscale(v[k], a.inv_n) : mk<V>((T)0, (T)0);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < N1; k++) {
+                    const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
+                                              : sph[k];
+                    v[k] = cmul2(v[k], p.hi, p.lo);
+                    if (tscaled) v[k] = cscale(v[k], tscale);
+                }
             }
             dft<N1, +1>(v);
         } else if constexpr (MODE == MODE_DIAG) {
@@ -564,7 +579,15 @@ pass_kernel(const PassArgs<T> a)
                 }
             }
             if constexpr (MODE == MODE_DIAG) continue;
-            if constexpr (MODE == MODE_FUSED) {
+            if constexpr (MODE == MODE_FUSED && kMask) {
+                const int lim = a.mask_lim[gg];
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++) {
+                    const int k = k1 + N1 * k2;
+                    const int kk = k < (N + 1) / 2 ? k : N - k;
+                    u[k2] = kk <= lim ? cscale(u[k2], a.inv_n) : mk<V>((T)0, (T)0);
+                }
+            } else if constexpr (MODE == MODE_FUSED) {
 #pragma unroll
                 for (int k2 = 0; k2 < N2; k2++) {
                     const int k = k1 + N1 * k2;

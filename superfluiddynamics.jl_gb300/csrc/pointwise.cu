@@ -133,32 +133,6 @@ cudaError_t launch_nl_term(const vec2<T> *q, const T *V, double beta, vec2<T> *t
     return cudaGetLastError();
 }
 
-// 2/3-rule mask of a natural-order spectrum (_dealias_scalar!, NSGP.jl:354-361):
-// cell e has last-axis index e / inner; its signed wavenumber index kk is kept
-// iff |kk| <= lim[e % inner] (the host evaluates the reference's Float64 test
-// sum xi^2 < xi_max for every mode and stores the largest kept |kk| per
-// inner position, -1 for none).
-template <typename T>
-__global__ void k_mask_spectrum(vec2<T> *__restrict__ f, const int *__restrict__ lim, int64_t n_last, int64_t inner,
-                                int64_t total)
-{
-    pdl_enter();
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t il = e / inner;
-        const int64_t kk = il < (n_last + 1) / 2 ? il : n_last - il;
-        if (kk > lim[e % inner]) f[e] = mk<vec2<T>>((T)0, (T)0);
-    }
-}
-
-template <typename T>
-cudaError_t launch_mask_spectrum(vec2<T> *f, const int *lim, int64_t n_last, int64_t inner, int64_t total,
-                                 cudaStream_t s)
-{
-    launch_pdl(k_mask_spectrum<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, f, lim, n_last, inner, total);
-    return cudaGetLastError();
-}
-
 // One RK stage from k = lapRot(q) and t = the (filtered) nonlinear term:
 //   kk = i (k - t)                                  (gp_rhs!)
 //   acc_mode 1: acc = kk; 2: acc = acc + acc_w kk   (k1 + 2k2 + 2k3 + k4, left to right)
@@ -199,10 +173,6 @@ template cudaError_t launch_nl_term<float>(const vec2<float> *, const float *, d
                                            cudaStream_t);
 template cudaError_t launch_nl_term<double>(const vec2<double> *, const double *, double, vec2<double> *, int64_t,
                                             cudaStream_t);
-template cudaError_t launch_mask_spectrum<float>(vec2<float> *, const int *, int64_t, int64_t, int64_t,
-                                                 cudaStream_t);
-template cudaError_t launch_mask_spectrum<double>(vec2<double> *, const int *, int64_t, int64_t, int64_t,
-                                                  cudaStream_t);
 template cudaError_t launch_rk_combine<float>(const vec2<float> *, const vec2<float> *, const vec2<float> *,
                                               vec2<float> *, vec2<float> *, int, double, double, int, int64_t,
                                               cudaStream_t);

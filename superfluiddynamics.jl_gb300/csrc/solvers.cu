@@ -48,26 +48,26 @@ static int rk_mask_table(gpss_ctx *c)
 }
 
 // in-place full transform of `f` (mul_all!/ldiv_all!): FWD x, y[, z] or INV z, y, x
-template <typename T> static int transform_all(gpss_ctx *c, void *f, bool inverse)
-{
-    for (int s = 0; s < c->ndim; s++) {
-        const int axis = inverse ? c->ndim - 1 - s : s;
-        PassArgs<T> a = axis_args<T>(c, axis, f, f);
-        GPSS_TRY(launch<T>(c, axis, inverse ? MODE_INV : MODE_FWD, a));
-    }
-    return GPSS_OK;
-}
-
+// The 2/3 filter (Plans.jl:529-532) of a field: forward transforms along the
+// leading axes, then one fused pass along the last axis (transform, keep the
+// modes inside the limit, inverse transform), then the inverse transforms
+// along the leading axes -- 2 ndim - 1 sweeps instead of 2 ndim + 1.
 template <typename T> static int dealias_field(gpss_ctx *c, void *f)
 {
     GPSS_TRY(rk_mask_table(c));
-    GPSS_TRY(transform_all<T>(c, f, false));
     const int last = c->ndim - 1;
-    cudaError_t e = launch_mask_spectrum<T>((vec2<T> *)f, c->rk_lim, c->n[last], c->total / c->n[last], c->total,
-                                            c->stream);
-    if (e != cudaSuccess) return fail(c, GPSS_ECUDA, "mask: %s", cudaGetErrorString(e));
-    c->launches++;
-    return transform_all<T>(c, f, true);
+    for (int axis = 0; axis < last; axis++) {
+        PassArgs<T> a = axis_args<T>(c, axis, f, f);
+        GPSS_TRY(launch<T>(c, axis, MODE_FWD, a));
+    }
+    PassArgs<T> m = axis_args<T>(c, last, f, f);
+    m.mask_lim = c->rk_lim;
+    GPSS_TRY(launch<T>(c, last, MODE_FUSED, m));
+    for (int axis = last - 1; axis >= 0; axis--) {
+        PassArgs<T> a = axis_args<T>(c, axis, f, f);
+        GPSS_TRY(launch<T>(c, axis, MODE_INV, a));
+    }
+    return GPSS_OK;
 }
 
 // out = lapRot(q) (GrossPitaevskii.jl:12-45) as one fused pass per axis with
