@@ -619,11 +619,12 @@ static cudaError_t run_stacks(gpss_batch *b, int nsteps, double dt, double *mass
         const float *V = b->d_V + st.off;
         const int fin_grid = (P + 127) / 128;
         auto mass = [&](int mode) -> cudaError_t {
-            launch_pdl(k_plane_mass, dim3(P * kPlaneChunks), dim3(kThreads), 0, b->stream, psi, cells, kPlaneChunks, st.d_partials);
+            launch_pdl(k_plane_mass, dim3(P * kPlaneChunks), dim3(kThreads), 0, b->stream, psi, cells, kPlaneChunks,
+                       st.d_partials);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
-            launch_pdl(k_plane_finish, dim3(fin_grid), dim3(128), 0, b->stream, st.d_partials, kPlaneChunks, P, mode, st.d_m0,
-                                                              st.d_scale, mass_out, st.d_plane_run, b->d_status);
+            launch_pdl(k_plane_finish, dim3(fin_grid), dim3(128), 0, b->stream, st.d_partials, kPlaneChunks, P, mode,
+                       st.d_m0, st.d_scale, mass_out, st.d_plane_run, b->d_status);
             return cudaGetLastError();
         };
         cudaError_t e = mass(0);

@@ -290,7 +290,8 @@ template <typename T>
 cudaError_t im_prep_be(const vec2<T> *phi, const T *V, double beta, double dt, int scheme, vec2<T> *M, T *Anl,
                        vec2<T> *b, int64_t total, cudaStream_t s)
 {
-    launch_pdl(k_im_prep_be<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, V, beta, 1.0 / dt, dt, scheme, M, Anl, b, total);
+    launch_pdl(k_im_prep_be<T>, dim3(im_grid(total)), dim3(256), 0, s,
+               phi, V, beta, 1.0 / dt, dt, scheme, M, Anl, b, total);
     return cudaGetLastError();
 }
 
@@ -298,7 +299,8 @@ template <typename T>
 cudaError_t im_prep_cn(const vec2<T> *phi, const vec2<T> *phi1, const T *V, double beta, double dt, int scheme,
                        vec2<T> *psim, T *Anl, vec2<T> *Anl2, vec2<T> *M, int64_t total, cudaStream_t s)
 {
-    launch_pdl(k_im_prep_cn<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, phi1, V, beta, 1.0 / dt, scheme, psim, Anl, Anl2, M, total);
+    launch_pdl(k_im_prep_cn<T>, dim3(im_grid(total)), dim3(256), 0, s,
+               phi, phi1, V, beta, 1.0 / dt, scheme, psim, Anl, Anl2, M, total);
     return cudaGetLastError();
 }
 
@@ -306,7 +308,8 @@ template <typename T>
 cudaError_t im_rhs_cn(const vec2<T> *phi, const vec2<T> *phi1, const vec2<T> *psim, const vec2<T> *lap, const T *V,
                       double beta, double dt, int tsch, vec2<T> *b, int64_t total, cudaStream_t s)
 {
-    launch_pdl(k_im_rhs_cn<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, phi1, psim, lap, V, beta, 1.0 / dt, tsch, b, total);
+    launch_pdl(k_im_rhs_cn<T>, dim3(im_grid(total)), dim3(256), 0, s,
+               phi, phi1, psim, lap, V, beta, 1.0 / dt, tsch, b, total);
     return cudaGetLastError();
 }
 
@@ -314,7 +317,8 @@ template <typename T>
 cudaError_t im_op(const vec2<T> *x, const vec2<T> *lap, int scheme, double dt, const vec2<T> *M, const T *Anl,
                   const vec2<T> *Anl2, const vec2<T> *b, int precond, vec2<T> *out, int64_t total, cudaStream_t s)
 {
-    launch_pdl(k_im_op<T>, dim3(im_grid(total)), dim3(256), 0, s, x, lap, scheme, 1.0 / dt, M, Anl, Anl2, b, precond, out, total);
+    launch_pdl(k_im_op<T>, dim3(im_grid(total)), dim3(256), 0, s,
+               x, lap, scheme, 1.0 / dt, M, Anl, Anl2, b, precond, out, total);
     return cudaGetLastError();
 }
 

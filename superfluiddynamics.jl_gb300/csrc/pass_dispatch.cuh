@@ -101,7 +101,8 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
         if constexpr (sizeof(T) == 4 && !XL && N >= 64) {
             // fewer default tiles than SMs: the 128-thread y/z instantiation
             if (blocks < sm_count()) {
-                if (adj && nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ | FEAT_NL | FEAT_SMALL>(a, blocks, s);
+                constexpr int kSmallAdjNL = FEAT_ADJ | FEAT_NL | FEAT_SMALL;
+                if (adj && nl) return launch_pass_inst<T, N, XL, MODE_FUSED, kSmallAdjNL>(a, blocks, s);
                 if (adj) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ADJ | FEAT_SMALL>(a, blocks, s);
                 if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_NL | FEAT_SMALL>(a, blocks, s);
                 return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_SMALL>(a, blocks, s);

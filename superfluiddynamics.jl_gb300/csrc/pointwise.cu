@@ -66,7 +66,8 @@ template <typename T>
 cudaError_t launch_mul_phase(vec2<T> *data, const vec2<T> *phase, int64_t prow, int axis,
                              const int64_t *n, int64_t total, cudaStream_t s)
 {
-    launch_pdl(k_mul_phase<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, data, phase, prow, axis, n[0], n[1], n[axis],
+    launch_pdl(k_mul_phase<T>, dim3(grid_for(total, 256)), dim3(256), 0, s,
+               data, phase, prow, axis, n[0], n[1], n[axis],
                                                         total);
     return cudaGetLastError();
 }
@@ -164,7 +165,8 @@ template <typename T>
 cudaError_t launch_rk_combine(const vec2<T> *k, const vec2<T> *t, const vec2<T> *psi0, vec2<T> *acc, vec2<T> *out,
                               int acc_mode, double acc_w, double cf, int from_acc, int64_t total, cudaStream_t s)
 {
-    launch_pdl(k_rk_combine<T>, dim3(grid_for(total, 256)), dim3(256), 0, s, k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc,
+    launch_pdl(k_rk_combine<T>, dim3(grid_for(total, 256)), dim3(256), 0, s,
+               k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc,
                                                          total);
     return cudaGetLastError();
 }
