@@ -166,8 +166,7 @@ cudaError_t launch_rk_combine(const vec2<T> *k, const vec2<T> *t, const vec2<T> 
                               int acc_mode, double acc_w, double cf, int from_acc, int64_t total, cudaStream_t s)
 {
     launch_pdl(k_rk_combine<T>, dim3(grid_for(total, 256)), dim3(256), 0, s,
-               k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc,
-                                                         total);
+               k, t, psi0, acc, out, acc_mode, (T)acc_w, (T)cf, from_acc, total);
     return cudaGetLastError();
 }
 
