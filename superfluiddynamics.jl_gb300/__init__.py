@@ -580,6 +580,11 @@ class BatchSplit2:
         return out
 
     def tuning(self):
+        """The launch choice: policy (0: runs up to 128^2 in shared memory, 1: up
+        to 64^2), queue order (0: largest first, 1: as given), stack level (runs
+        of one size and box as planes through the pass kernels: 1 the 256^2
+        runs, 2 also 128^2, 3 every size) and the 16 trial times in ms (index
+        4 stack + 2 policy + order; 1e30 for candidates not tried)."""
         pol, order, stack = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         ms = (ctypes.c_float * 16)()
         self._ck(_lib.lib().gpss_batch_tuning(self._h, ctypes.byref(pol), ctypes.byref(order), ctypes.byref(stack),
@@ -587,7 +592,7 @@ class BatchSplit2:
         return {"policy": pol.value, "order": order.value, "stack": stack.value, "trial_ms": list(ms)}
 
     def set_tuning(self, policy, order, stack=0):
-        """Fix the launch choice (skips the autotuner)."""
+        """Fix the launch choice (skips the autotuner); stack level 0 to 3."""
         self._ck(_lib.lib().gpss_batch_set_tuning(self._h, int(policy), int(order), int(stack)))
 
     def close(self):
