@@ -32,7 +32,7 @@ template <typename T, int N, bool XL, int MODE, int FEAT = FEAT_ALL>
 static cudaError_t launch_pass_inst(const PassArgs<T> &a, int tiles, cudaStream_t s)
 {
     using S = PassShape<T, N, XL, FEAT>;
-    if (FEAT & FEAT_SMALL) tiles = (a.nlines + S::W - 1) / S::W;  // the host counted default tiles
+    tiles = (a.nlines + S::W - 1) / S::W;  // this instantiation's tiles (the host counts default ones)
     auto k = pass_kernel<T, N, XL, MODE, FEAT>;
     static int wave[64] = {0};
     int dev = 0;

@@ -217,9 +217,16 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 // Small fields (a 2D y pass of 256 columns is 16 tiles of 16): y/z CTAs of 128
 // threads give twice the tiles (2D 128^2 step 11.4 -> 10.6 us, 256^2 13.1 ->
 // 12.5 us); at 256^3 they would cost the y pass 34 %.
+// (the lean y/z pass in CTAs of 512 threads, 32 columns = 256 B runs, 2 per
+// SM: y 63.0 -> 67.8 us at 256^3)
+#ifndef GPSS_PASS_THREADS_COL_LEAN_F32
+#define GPSS_PASS_THREADS_COL_LEAN_F32 256
+#endif
 template <typename T, bool XL, int FEAT = 0> struct PassGeom {
     static constexpr int THREADS =
-        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32 : ((FEAT & FEAT_SMALL) ? 128 : GPSS_PASS_THREADS_COL_F32))
+        sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32
+                             : ((FEAT & FEAT_SMALL) ? 128
+                                : (FEAT == FEAT_NONE ? GPSS_PASS_THREADS_COL_LEAN_F32 : GPSS_PASS_THREADS_COL_F32)))
                        : GPSS_PASS_THREADS_F64;
 };
 // The merged imaginary-time passes (FEAT_IMAGM) fit 72 (x) and 64 (y/z)
