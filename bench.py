@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the accuracy, cfg2, cfg4 and cuFFT measurements")
-    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve"], default=None,
+    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve", "implicit"], default=None,
                     help="run one secondary measurement alone and print it (profiling runs)")
     ap.add_argument("--only-steps", type=int, default=None,
                     help="with --only imag/solve: time steps (iterations) to time")
@@ -384,6 +384,27 @@ def measure_solve(sfd, c, iters=20):
     return out
 
 
+def measure_implicit(sfd, W, steps=4):
+    """The implicit schemes (imaginary-time BE and CN with the reference's
+    BiCGStab) on the cfg2 physics at 64^3, FP64: time per step and Krylov
+    iterations per step (each iteration reads its FP64 dot products back)."""
+    c = W.cfg2(64)
+    out = {"workload": f"cfg2 physics at 64^3 (trap, g=2000), FP64, dt=1e-3, {steps} steps per timing"}
+    for name, cls in (("backward_euler", sfd.NumModelBackwardEuler), ("crank_nicolson", sfd.NumModelCrankNicolson)):
+        grid = sfd.Grid(c["shape"], c["bounds"])
+        f = sfd.Field(grid)
+        f.phi = c["psi"]
+        p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, c["V"]), coeffD=c["coeffD"], beta=c["beta"])
+        m = cls(f, p, c["dt"], steps, steps, precision="fp64")
+        m.step(1)
+        t0 = time.perf_counter()
+        m.step(steps)
+        t = time.perf_counter() - t0
+        out[name] = {"ms_per_step": t / steps * 1e3, "krylov_iterations_per_step": m.last_krylov / steps}
+        m.close(download=False)
+    return out
+
+
 def run_only(args):
     """One secondary measurement alone (for profiling it), one JSON line."""
     import importlib
@@ -400,6 +421,8 @@ def run_only(args):
         r = measure_batch(sfd, W)
     elif args.only == "rk4":
         r = measure_rk(sfd, W.cfg1(256), L)
+    elif args.only == "implicit":
+        r = measure_implicit(sfd, W)
     else:
         r = measure_solve(sfd, W.cfg1(256), iters=args.only_steps or 20)
     print(json.dumps(r), flush=True)
@@ -578,6 +601,7 @@ def run_gpss(args, rank, world, local):
         extra["adjoint"] = measure_adjoint(sfd, W)
         extra["rk4"] = measure_rk(sfd, c, L)
         extra["solve"] = measure_solve(sfd, c)
+        extra["implicit"] = measure_implicit(sfd, W)
         cu = measure_cufft(c, args.n)
         if cu:
             cu["gpss_pass_ms"] = per_axis
