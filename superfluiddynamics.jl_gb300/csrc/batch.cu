@@ -738,7 +738,10 @@ int gpss_batch_create(gpss_batch **out, int nruns, const int64_t *n, const doubl
         }
         st.count = (int)st.runs.size();
         st.level = st.n == 256 ? 1 : (st.n == 128 ? 2 : 3);
-        if (st.count >= 2) b->stacks.push_back(st);
+        // the pass kernels index a field with 32 bits: larger stacks stay in
+        // the persistent launch (64-bit run offsets)
+        const bool fits = (int64_t)st.count * st.n * st.n < (int64_t(1) << 31);
+        if (st.count >= 2 && fits) b->stacks.push_back(st);
     }
     b->total = off;
     auto stacked = [&](int r, int mode) {
