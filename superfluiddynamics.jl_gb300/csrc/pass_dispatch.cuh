@@ -79,25 +79,27 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
     case MODE_FUSED: {
         // the leanest instantiation that does everything the arguments ask for
         const bool adj = a.pre_out != nullptr || a.adj_pre != nullptr;
-        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0 || a.acc != nullptr;
+        const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0;
+        const bool acc = a.acc != nullptr;
         const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
         if (a.mask_lim) {
-            if (diag || adj || nl || a.nl_pre || a.dot_with) return cudaErrorInvalidValue;
+            if (diag || acc || adj || nl || a.nl_pre || a.dot_with) return cudaErrorInvalidValue;
             return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_MASK>(a, blocks, s);
         }
         if (!a.phase) return cudaErrorInvalidValue;  // every other fused pass reads a phase table
         if (a.nl_pre || a.dot_with) {
-            if (diag || adj || a.nl_mode != NL_NONE) return cudaErrorInvalidValue;
+            if (diag || acc || adj || a.nl_mode != NL_NONE) return cudaErrorInvalidValue;
             return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_IMAGM>(a, blocks, s);
         }
         if constexpr (sizeof(T) == 4 && N >= 64) {
             if (a.plane_nl || a.plane_scale) {
-                if (diag || adj) return cudaErrorInvalidValue;  // planes carry no energy sums, rotation or adjoint
+                if (diag || acc || adj) return cudaErrorInvalidValue;  // planes: no energy sums, rotation, adjoint
                 if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_PLANE | FEAT_NL>(a, blocks, s);
                 return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_PLANE>(a, blocks, s);
             }
         }
-        if (diag) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
+        if (diag || (acc && (adj || nl))) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
+        if (acc) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ACC>(a, blocks, s);
         if constexpr (sizeof(T) == 4 && !XL && N >= 64) {
             // fewer default tiles than SMs: the 128-thread y/z instantiation
             if (blocks < sm_count()) {

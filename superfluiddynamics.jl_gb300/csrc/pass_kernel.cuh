@@ -85,8 +85,10 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //   FEAT_MASK  the 2/3 dealiasing filter in place of the phase: on the last
 //              axis of a spectrum already transformed along the others, keep
 //              the modes with |kk| <= mask_lim[line] (scaled by 1/n), zero the rest
+//   FEAT_ACC   the `acc` epilogue alone (add the result to a second field:
+//              the y/z passes of lapRot in the RK and implicit schemes)
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
-       FEAT_SMALL = 32, FEAT_MASK = 64 };
+       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -375,6 +377,7 @@ pass_kernel(const PassArgs<T> a)
     constexpr bool kImagM = (FEAT & FEAT_IMAGM) != 0;
     constexpr bool kAdj = kDiag || (FEAT & FEAT_ADJ) != 0;
     constexpr bool kMask = (FEAT & FEAT_MASK) != 0;
+    constexpr bool kAcc = kDiag || (FEAT & FEAT_ACC) != 0;
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -761,7 +764,7 @@ pass_kernel(const PassArgs<T> a)
             }
         }
         if (valid) {
-            if (MODE == MODE_FUSED && kDiag && a.acc) {
+            if (MODE == MODE_FUSED && kAcc && a.acc) {
 #pragma unroll
                 for (int j = 0; j < N1; j++) {
                     const uint32_t e = base + (uint32_t)(r + N2 * j) * st;
