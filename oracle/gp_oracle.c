@@ -1,6 +1,6 @@
 /*
  * gp_oracle.c -- CPU restatement of SuperfluidDynamics.jl's split-step
- * Gross-Pitaevskii path, used as the CHECKER of the CUDA library.
+ * Gross-Pitaevskii path: the oracle the CUDA library is tested against.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference arm of bench.py load this file's library.  The

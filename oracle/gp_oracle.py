@@ -9,7 +9,7 @@ Two independent FP64 restatements of SuperfluidDynamics.jl's `NumModelSplit1` /
   second FFT implementation, for small cross-checks.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline arm use
-this module, and only as the checker.  Fields are numpy arrays of shape
+this module, and only as the oracle.  Fields are numpy arrays of shape
 ``(nx, ny[, nz])`` in Fortran order, i.e. x fastest in memory like the
 reference's Julia ``Array{ComplexF64}``.
 """

@@ -16,7 +16,7 @@ cfg2  3D 128^3 on [-10,10]^3, V = (x^2 + y^2 + 4 z^2)/2, beta = 2000, imaginary
       time; psi0 = unit-mass Gaussian + U(-1e-3, 1e-3) noise on re and im,
       renormalised; dt = 1e-3.
 cfg3  512 independent 2D runs: 256 x 64^2, 192 x 128^2, 64 x 256^2, all on
-      [-8,8]^2 (the box is this build's choice), V = (a x^2 + b y^2)/2 with
+      [-8,8]^2 (a box chosen here; the workload gives none), V = (a x^2 + b y^2)/2 with
       a, b ~ U(0.5, 2) plus 8 Gaussian bumps (heights U(0, 2), centres
       U(-6, 6)^2, width 0.5), g ~ U(100, 1000), psi0 = the trap's oscillator
       ground state times a cfg0-style phase imprint, unit mass; dt = 1e-3,
