@@ -217,10 +217,10 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #define GPSS_PASS_THREADS_F64 64
 #endif
 // Small fields (a 2D y pass of 256 columns is 16 tiles of 16): y/z CTAs of 128
-// threads give twice the tiles (2D 128^2 step 11.4 -> 10.6 us, 256^2 13.1 ->
-// 12.5 us); at 256^3 they would cost the y pass 34 %.
-// (the lean y/z pass in CTAs of 512 threads, 32 columns = 256 B runs, 2 per
-// SM: y 63.0 -> 67.8 us at 256^3)
+// threads (FEAT_SMALL) give twice the tiles (2D 128^2 step 11.4 -> 10.6 us,
+// 256^2 13.1 -> 12.5 us); at 256^3 they would cost the y pass 34 %.  The lean
+// y/z pass in CTAs of 512 threads (32 columns = 256 B runs, 2 per SM) was
+// slower too: y 63.0 -> 67.8 us at 256^3.
 #ifndef GPSS_PASS_THREADS_COL_LEAN_F32
 #define GPSS_PASS_THREADS_COL_LEAN_F32 256
 #endif
@@ -233,8 +233,8 @@ template <typename T, bool XL, int FEAT = 0> struct PassGeom {
 };
 // The merged imaginary-time passes (FEAT_IMAGM) fit 72 (x) and 64 (y/z)
 // registers without spills; with one more CTA per SM a 128^3 field's x pass
-// (1024 tiles) runs in one round instead of 1.12 (912 slots): cfg2 step
-// 38.8 -> 34.6 us.
+// (1024 tiles) fits one wave of resident CTAs (1064) instead of 1.12 waves
+// of 912: the 128^3 imaginary-time trap step 38.8 -> 34.6 us.
 #ifndef GPSS_PASS_SM_THREADS_IMAGM_XL_F32
 #define GPSS_PASS_SM_THREADS_IMAGM_XL_F32 896
 #endif
@@ -242,7 +242,9 @@ template <typename T, bool XL, int FEAT = 0> struct PassGeom {
 #define GPSS_PASS_SM_THREADS_IMAGM_F32 1024
 #endif
 #ifndef GPSS_PASS_SM_THREADS_PLANE_XL_F32
-#define GPSS_PASS_SM_THREADS_PLANE_XL_F32 896  // stacked planes: cfg3 44.1 -> 43.5 ms per 500 steps
+// stacked 2D planes: 7 CTAs per SM give 64 x 256^2 planes' 2048 x tiles 1.9
+// waves instead of 2.25 (the 512-run batch 44.1 -> 43.5 ms per 500 steps)
+#define GPSS_PASS_SM_THREADS_PLANE_XL_F32 896
 #endif
 template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
     static constexpr int SM_THREADS =
