@@ -913,7 +913,7 @@ int gpss_batch_step(gpss_batch *b, int nsteps, double dt, double *mass_out)
         }
         // Near-ties go to policy 0: its runs stay in shared memory, while
         // policy 1's tiled 128^2 runs share L2 and its full-length time varies
-        // from call to call (cfg3: 51 to 59 ms per 500 steps for a candidate
+        // from call to call (the 512-run batch: 51 to 59 ms per 500 steps for a candidate
         // whose 16-step trials matched policy 0's within 1%).
         if (b->policy == 1) {
             const int twin = (b->stack_mode << 2) | b->order_mode;
