@@ -121,3 +121,21 @@ def test_build_recipe_targets_sm103a(sfd):
     m = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(m)
     assert "arch=compute_103a,code=sm_103a" in m.ARCH
+
+
+def test_overlap_loss_checks_arguments_on_the_host(sfd):
+    """The autograd wrapper of gpss_adjoint rejects mismatched shapes and
+    dtypes before any call into the library."""
+    import importlib
+    import types
+    torch = pytest.importorskip("torch")
+    AD = importlib.import_module("sfd_gb300.autodiff")
+    model = types.SimpleNamespace(f=types.SimpleNamespace(g=types.SimpleNamespace(n=(8, 8))))
+    V = torch.zeros(8, 8, dtype=torch.float64)
+    psi = torch.zeros(8, 8, dtype=torch.complex128)
+    with pytest.raises(ValueError):
+        AD.overlap_loss(model, torch.zeros(8, 4, dtype=torch.float64), psi, None, 1)
+    with pytest.raises(TypeError):
+        AD.overlap_loss(model, psi, psi, None, 1)
+    with pytest.raises(TypeError):
+        AD.overlap_loss(model, V, V, None, 1)

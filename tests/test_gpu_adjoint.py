@@ -169,3 +169,32 @@ def test_adjoint_golden_cfg4_32(sfd, W):
     for dv, dpsi, dL in zip(z["dV"], z["dpsi0"], z["dL"]):
         adj = float(np.sum(dLdV * dv)) + float(np.real(np.sum(np.conj(g0) * dpsi)))
         assert abs(adj - dL) <= 1e-8 * abs(dL)
+
+
+def test_overlap_loss_autograd_function(sfd, W):
+    """overlap_loss as a torch.autograd.Function: its loss and gradients are
+    those of gpss_adjoint, they chain through other torch operations, and a
+    central difference of the function itself agrees with the gradient."""
+    import importlib
+    torch = pytest.importorskip("torch")
+    AD = importlib.import_module("sfd_gb300.autodiff")
+    c = W.cfg4(32)
+    nsteps, K = 40, 7
+    f, n = _model(sfd, c, c["V"])
+    L_ref, dV_ref, g_ref = n.adjoint(c["target"], nsteps, K)
+    V = torch.tensor(np.ascontiguousarray(c["V"]), dtype=torch.float64, requires_grad=True)
+    psi0 = torch.tensor(np.ascontiguousarray(c["psi"]), dtype=torch.complex128, requires_grad=True)
+    L = AD.overlap_loss(n, V, psi0, c["target"], nsteps, K)
+    (3.0 * L + (V * V).sum()).backward()
+    assert abs(L.item() - L_ref) < 1e-14
+    assert np.allclose(V.grad.numpy(), 3.0 * dV_ref + 2.0 * c["V"], rtol=0, atol=1e-13 * np.abs(dV_ref).max())
+    assert np.allclose(psi0.grad.numpy(), 3.0 * g_ref, rtol=0, atol=1e-13 * np.abs(g_ref).max())
+    # central difference through the function along one smooth direction of V
+    dv = torch.tensor(np.ascontiguousarray(_directions(c["shape"], 1, seed=17)[0]))
+    eps = 1e-4
+    with torch.no_grad():
+        lp = AD.overlap_loss(n, V + eps * dv, psi0, c["target"], nsteps, K).item()
+        lm = AD.overlap_loss(n, V - eps * dv, psi0, c["target"], nsteps, K).item()
+    adj = float((torch.from_numpy(np.ascontiguousarray(dV_ref)) * dv).sum())
+    assert abs((lp - lm) / (2 * eps) - adj) <= 1e-6 * abs(adj)
+    n.close()
