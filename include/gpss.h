@@ -31,6 +31,7 @@ extern "C" {
 #define GPSS_ENONFINITE (-4)  /* a reduction saw NaN/Inf in the field */
 #define GPSS_ETIMEOUT (-5)    /* a bounded device-side wait gave up */
 #define GPSS_ESTATE (-6)      /* call out of order (e.g. no field uploaded) */
+#define GPSS_EIO (-7)         /* a file could not be read or written, or holds an unread form */
 
 /* precision of the device field and of the FFT/phase arithmetic */
 #define GPSS_FP64 64
@@ -186,6 +187,32 @@ int gpss_ground_state(gpss_ctx *ctx, double dt, double tol, int64_t max_steps, i
  */
 int gpss_adjoint(gpss_ctx *ctx, const double *psi_target, int nsteps, int K, double dt, double *loss,
                  double *dLdV, double *dLdpsi0);
+
+/* ---- HDF5 checkpoints ----
+ *
+ * The file WriterSave writes and reads (src/IO/Writers.jl:41-92 write!,
+ * :115-137 read!), "<prefix>-<istep>.h5": float64 datasets "re" and "im" in
+ * the root group, the dataspace listing Julia's (nx, ny[, nz]) in reverse
+ * (HDF5 is row-major), bytes in the field's own order (x fastest).  Written
+ * without an HDF5 library (classic format structures: superblock 0, v1 object
+ * headers, a symbol-table group, contiguous storage); read back from files
+ * of that classic form as the HDF5 library writes them (user block,
+ * continuation blocks, multi-level group B-trees, contiguous or compact
+ * float32/float64 storage).  Other forms return GPSS_EIO with a message.
+ */
+
+/* Download the device field and write it (write!(WriterSave(f); prefix, istep)). */
+int gpss_write_h5(gpss_ctx *ctx, const char *path);
+/* Read "re"/"im" of the field's shape and upload them (read!(WriterSave(f); ...)). */
+int gpss_read_h5(gpss_ctx *ctx, const char *path);
+/* The same for a host field (interleaved complex doubles, n[0..ndim-1] = nx, ny[, nz]);
+ * messages go to gpss_last_error(NULL). */
+int gpss_h5_write_field(const char *path, int ndim, const int64_t *n, const double *psi);
+int gpss_h5_read_field(const char *path, int ndim, const int64_t *n, double *psi);
+/* Any float dataset of the root group: rank and dims (slowest first, up to 8)
+ * always; values as doubles into out[0..cap) when out is not NULL. */
+int gpss_h5_read_dataset(const char *path, const char *name, int *rank, int64_t *dims, double *out,
+                         int64_t cap);
 
 /* ---- batched runs (an extension: the reference integrates one field at a time) ---- */
 

@@ -17,6 +17,7 @@ reference (Julia)                      here
 ``timeStep!(n)``                       ``timeStep(n[, nsteps])`` (splitting.jl:78, 149)
 ``energy(n[, show])``                  ``energy(n[, show])``    (GrossPitaevskii.jl:61, 106)
 ``solve!(n; istart)``                  ``solve(n, istart=1)``   (NumModels.jl:23-46)
+``write!/read!(WriterSave(f); ...)``   ``WriterSave(f).write/read(prefix, istep)`` (Writers.jl:41-137)
 =====================================  =============================================
 
 Fields are numpy arrays of shape ``(nx, ny[, nz])`` in Fortran order: x is
@@ -40,7 +41,7 @@ __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "P
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
            "solve", "BatchSplit2", "GPSSError", "version", "NumModelGPRK", "NumModelBackwardEuler", "NumModelBackwardEulerNoPrecond",
            "NumModelCrankNicolson", "NumModelCrankNicolsonQuasiNewton", "NumModelCrankNicolsonT",
-           "NumModelCrankNicolsonQuasiNewtonT"]
+           "NumModelCrankNicolsonQuasiNewtonT", "WriterSave", "read_h5_dataset"]
 
 _f64p = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -505,6 +506,66 @@ def energy(n: _SplitModel, show: bool = False):
 def chemical_potential(n: _SplitModel) -> float:
     """mu = -E_Omega + E_Delta + 2 E_beta (GrossPitaevskii.jl:79)."""
     return n.energies()[4]
+
+
+class WriterSave:
+    """WriterSave(f) (Writers.jl:17-20; write! :41-92, read! :115-137): the
+    field as "<prefix>-<istep>.h5" holding float64 datasets "re" and "im"
+    (dataspace (nz, ny, nx) / (ny, nx), x fastest, as Julia writes its
+    column-major arrays).  A field owned by a model is written from the
+    device buffer and read straight back into it; the library writes the
+    HDF5 structures itself (gpss_write_h5 / gpss_h5_write_field).  An
+    instance is also a writer hook for ``solve``."""
+
+    def __init__(self, f: Field):
+        self.f = f
+
+    @staticmethod
+    def path(prefix="res", istep=0):
+        return f"{prefix}-{int(istep)}.h5"
+
+    def _shape(self):
+        g = self.f.g
+        return g.ndim, (ctypes.c_int64 * 3)(*(list(g.n) + [1] * (3 - g.ndim)))
+
+    def write(self, prefix="res", istep=0, dt=1.0):
+        path = self.path(prefix, istep).encode()
+        owner = self.f._owner
+        if owner is not None and owner._h:
+            owner._ck(_lib.lib().gpss_write_h5(owner._h, path))
+            return
+        nd, n = self._shape()
+        a = np.asfortranarray(self.f._phi, dtype=np.complex128)
+        _lib.check(_lib.lib().gpss_h5_write_field(path, nd, n, a.ctypes.data_as(_f64p)))
+
+    def read(self, prefix="res", istep=0, dt=1.0):
+        path = self.path(prefix, istep).encode()
+        owner = self.f._owner
+        if owner is not None and owner._h:
+            owner._ck(_lib.lib().gpss_read_h5(owner._h, path))
+            owner._device_newer = True  # the host copy is stale until read
+            return
+        nd, n = self._shape()
+        a = np.zeros(self.f.g.n, dtype=np.complex128, order="F")
+        _lib.check(_lib.lib().gpss_h5_read_field(path, nd, n, a.ctypes.data_as(_f64p)))
+        self.f._phi = a
+
+    def __call__(self, field, prefix, istep, dt):
+        self.write(prefix, istep, dt)
+
+
+def read_h5_dataset(path, name):
+    """Any float dataset of an HDF5 file's root group, as a float64 array of
+    the dataset's (row-major) shape."""
+    L = _lib.lib()
+    rank = ctypes.c_int()
+    dims = (ctypes.c_int64 * 8)()
+    _lib.check(L.gpss_h5_read_dataset(str(path).encode(), name.encode(), ctypes.byref(rank), dims, None, 0))
+    shape = tuple(dims[i] for i in range(rank.value))
+    out = np.zeros(shape, dtype=np.float64)
+    _lib.check(L.gpss_h5_read_dataset(str(path).encode(), name.encode(), ctypes.byref(rank), dims,
+                                      out.ctypes.data_as(_f64p), out.size))
+    return out
 
 
 def solve(n: _SplitModel, istart: int = 1):

@@ -21,6 +21,7 @@ GPSS_ECUDA = -3
 GPSS_ENONFINITE = -4
 GPSS_ETIMEOUT = -5
 GPSS_ESTATE = -6
+GPSS_EIO = -7
 GPSS_FP64 = 64
 GPSS_FP32 = 32
 GPSS_FLAG_PLAIN = 1
@@ -32,7 +33,8 @@ GPSS_LIE = 1
 GPSS_STRANG = 2
 
 _CODES = {GPSS_EINVAL: "EINVAL", GPSS_ENOMEM: "ENOMEM", GPSS_ECUDA: "ECUDA",
-          GPSS_ENONFINITE: "ENONFINITE", GPSS_ETIMEOUT: "ETIMEOUT", GPSS_ESTATE: "ESTATE"}
+          GPSS_ENONFINITE: "ENONFINITE", GPSS_ETIMEOUT: "ETIMEOUT", GPSS_ESTATE: "ESTATE",
+          GPSS_EIO: "EIO"}
 
 
 class GPSSError(RuntimeError):
@@ -76,6 +78,12 @@ SIGNATURES = {
                                          ctypes.c_int, _f64p, _i64p]),
     "gpss_adjoint": (ctypes.c_int, [_vp, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_double, _f64p, _f64p,
                                     _f64p]),
+    "gpss_write_h5": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "gpss_read_h5": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "gpss_h5_write_field": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _i64p, _f64p]),
+    "gpss_h5_read_field": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _i64p, _f64p]),
+    "gpss_h5_read_dataset": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _i64p,
+                                            _f64p, ctypes.c_int64]),
     "gpss_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double]),
     "gpss_batch_destroy": (None, [_vp]),
     "gpss_batch_last_error": (ctypes.c_char_p, [_vp]),
