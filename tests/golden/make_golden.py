@@ -12,7 +12,9 @@ steps), cfg2 at 32^3 (200 imaginary-time steps), two cfg3 runs at 64^2 (seeds 0 
 steps) and the cfg4 gradient workload at 32^2 (`cfg4_grad_32.grad.npz`: the
 loss and its directional derivatives along seeded (dV, dpsi0) directions from
 the oracle's dual-number restatement, checked here against central
-differences of the FP64 oracle).
+differences of the FP64 oracle).  The `*.solver.npz` fixtures hold explicit
+RK and implicit (Backward-Euler, Crank-Nicolson) runs of the oracle, each
+cross-checked against the numpy restatement (and its Krylov count).
 
 Run from the repository root on an x86 host (80-bit long double):
     python tests/golden/make_golden.py
@@ -150,7 +152,50 @@ def grad_case():
     print("cfg4_grad_32", "L", L, "dL", dLs)
 
 
+def solver_cases():
+    """Fixtures of the integrators beside the split step: NumModelGPRK
+    (explicit-rk.jl:96-166) and the implicit Krylov schemes
+    (backward-euler.jl, crank-nicolson.jl, krylov.jl)."""
+    b2 = ((-6.0, 6.0), (-4.0, 5.0))
+    V2 = O.quadratic_potential((64, 32), b2)
+    yield "rk4_product_2d_rot", dict(kind="rk", psi0=0.5 * field((64, 32), 11), bounds=b2, V=V2, coeffD=-0.5,
+                                     beta=2.0, omega=0.6, nsteps=20, dt=1e-3, stepper="RK4", filter="product")
+    b3 = ((-4.0, 4.0), (-3.0, 3.0), (-2.0, 2.0))
+    yield "rk2_solution_3d", dict(kind="rk", psi0=0.5 * field((32, 16, 16), 12), bounds=b3,
+                                  V=O.quadratic_potential((32, 16, 16), b3), coeffD=-0.5, beta=2.0, omega=0.3,
+                                  nsteps=12, dt=1e-3, stepper="RK2", filter="solution")
+    b = ((-6.0, 6.0), (-6.0, 6.0))
+    p0 = field((32, 32), 13)
+    p0 = np.asfortranarray(p0 / O.c_norm(p0, b))
+    for scheme in ("BackwardEuler", "CrankNicolson"):
+        yield f"{scheme.lower()}_2d", dict(kind="implicit", psi0=p0, bounds=b, V=O.quadratic_potential((32, 32), b),
+                                          coeffD=-0.5, beta=5.0, omega=0.0, nsteps=3, dt=1e-2, scheme=scheme)
+
+
+def solver_main():
+    for name, c in solver_cases():
+        kw = dict(coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"], nsteps=c["nsteps"], dt=c["dt"])
+        extra = {}
+        if c["kind"] == "rk":
+            kw.update(stepper=c["stepper"], filter=c["filter"])
+            out = O.c_rk_step(c["psi0"], c["bounds"], **kw)
+            chk = O.np_rk_step(c["psi0"], c["bounds"], **kw)
+            extra = dict(stepper=c["stepper"], filter=c["filter"])
+        else:
+            kw.update(scheme=c["scheme"])
+            out, iters = O.c_implicit_step(c["psi0"], c["bounds"], **kw)
+            chk, iters_np = O.np_implicit_step(c["psi0"], c["bounds"], **kw)
+            assert iters == iters_np, name
+            extra = dict(scheme=c["scheme"], krylov=iters)
+        assert O.rel_l2(out, chk) < 1e-11, (name, O.rel_l2(out, chk))
+        np.savez_compressed(os.path.join(HERE, name + ".solver.npz"), kind=c["kind"], psi0=c["psi0"], psi=out,
+                            V=c["V"], bounds=np.array(c["bounds"]), coeffD=c["coeffD"], beta=c["beta"],
+                            omega=c["omega"], nsteps=c["nsteps"], dt=c["dt"], **extra)
+        print(name, out.shape, "numpy vs C oracle", O.rel_l2(out, chk), extra.get("krylov", ""))
+
+
 def main():
+    solver_main()
     grad_case()
     for name, c in cases():
         kw = dict(coeffD=c["coeffD"], beta=c["beta"], omega=c["omega"], V=c["V"], nsteps=c["nsteps"],

@@ -73,6 +73,28 @@ def test_implicit_fp32(sfd, O, scheme):
     assert O.rel_l2(got, want) < 1e-5
 
 
+def _solver_fixture(name):
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".solver.npz"))
+    return z, tuple(tuple(r) for r in z["bounds"])
+
+
+@pytest.mark.parametrize("name", ["backwardeuler_2d", "cranknicolson_2d"])
+def test_implicit_golden(sfd, name):
+    """The committed implicit-scheme fixtures (the oracle's field and Krylov
+    count after 3 steps)."""
+    z, b = _solver_fixture(name)
+    kw = dict(coeffD=float(z["coeffD"]), beta=float(z["beta"]), omega=float(z["omega"]), dt=float(z["dt"]))
+    got, ng = run_implicit(sfd, str(z["scheme"]), z["psi0"].shape, b, z["psi0"], z["V"], nsteps=int(z["nsteps"]),
+                           **kw)
+    err = np.linalg.norm(got - z["psi"]) / np.linalg.norm(z["psi"])
+    if ng == int(z["krylov"]):
+        assert err < 1e-10
+    else:
+        assert abs(ng - int(z["krylov"])) <= 3
+        assert err < 1e-7, (ng, int(z["krylov"]), err)
+
+
 def test_implicit_rejects_bad_arguments(sfd):
     from sfd_gb300 import _lib
     g = sfd.Grid((16, 16), ((0.0, 1.0), (0.0, 1.0)))

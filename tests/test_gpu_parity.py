@@ -339,7 +339,7 @@ def _golden():
     import os
     here = os.path.join(os.path.dirname(__file__), "golden")
     return sorted(os.path.join(here, f) for f in os.listdir(here)
-                  if f.endswith(".npz") and not f.endswith(".grad.npz"))
+                  if f.endswith(".npz") and not f.endswith((".grad.npz", ".solver.npz")))
 
 
 @pytest.mark.parametrize("path", _golden(), ids=lambda p: p.split("/")[-1][:-4])

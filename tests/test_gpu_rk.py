@@ -85,3 +85,18 @@ def test_rk_rejects_bad_arguments(sfd):
     assert _lib.lib().gpss_rk_step(n.handle, 1, 3, 1, 1e-3) == -1
     assert _lib.lib().gpss_rk_step(n.handle, 1, 4, 7, 1e-3) == -1
     n.close()
+
+
+@pytest.mark.parametrize("name", ["rk4_product_2d_rot", "rk2_solution_3d"])
+def test_rk_golden(sfd, name):
+    """The committed explicit-RK fixtures (the oracle's field): FP64 within
+    1e-12, FP32 within 1e-5."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".solver.npz"))
+    b = tuple(tuple(r) for r in z["bounds"])
+    kw = dict(coeffD=float(z["coeffD"]), beta=float(z["beta"]), omega=float(z["omega"]), dt=float(z["dt"]),
+              stepper=str(z["stepper"]), filter=str(z["filter"]))
+    want = z["psi"]
+    for precision, tol in (("fp64", 1e-12), ("fp32", 1e-5)):
+        got = run_rk(sfd, want.shape, b, z["psi0"], V=z["V"], precision=precision, nsteps=int(z["nsteps"]), **kw)
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < tol, precision

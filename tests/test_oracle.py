@@ -163,7 +163,7 @@ def test_golden_fixtures_reproduce(O):
     """The committed golden vectors (tests/golden/) are what the oracle computes."""
     import os
     here = os.path.join(os.path.dirname(__file__), "golden")
-    names = sorted(f for f in os.listdir(here) if f.endswith(".npz") and not f.endswith(".grad.npz"))
+    names = sorted(f for f in os.listdir(here) if f.endswith(".npz") and not f.endswith((".grad.npz", ".solver.npz")))
     assert names, "no golden fixtures"
     for nm in names:
         z = np.load(os.path.join(here, nm))
@@ -213,3 +213,32 @@ def test_golden_gradient_reproduces(O):
                                  dt=float(z["dt"]))
         assert abs(L - float(z["L"])) < 1e-13
         assert abs(d - dL) <= 1e-12 * abs(dL)
+
+
+def _solver_fixtures():
+    import os
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    return sorted(os.path.join(here, f) for f in os.listdir(here) if f.endswith(".solver.npz"))
+
+
+def test_solver_fixtures_present():
+    import os
+    names = {os.path.basename(p) for p in _solver_fixtures()}
+    assert names == {"rk4_product_2d_rot.solver.npz", "rk2_solution_3d.solver.npz", "backwardeuler_2d.solver.npz",
+                     "cranknicolson_2d.solver.npz"}
+
+
+@pytest.mark.parametrize("path", _solver_fixtures(), ids=lambda p: p.rsplit("/", 1)[-1])
+def test_golden_solver_reproduces(O, path):
+    """The committed explicit-RK and implicit-scheme fixtures: the oracle
+    reproduces the field (and the implicit schemes' Krylov count)."""
+    z = np.load(path)
+    b = tuple(tuple(r) for r in z["bounds"])
+    kw = dict(coeffD=float(z["coeffD"]), beta=float(z["beta"]), omega=float(z["omega"]), V=z["V"],
+              nsteps=int(z["nsteps"]), dt=float(z["dt"]))
+    if str(z["kind"]) == "rk":
+        out = O.c_rk_step(z["psi0"], b, stepper=str(z["stepper"]), filter=str(z["filter"]), **kw)
+    else:
+        out, iters = O.c_implicit_step(z["psi0"], b, scheme=str(z["scheme"]), **kw)
+        assert iters == int(z["krylov"])
+    assert O.rel_l2(out, z["psi"]) < 1e-14
