@@ -22,6 +22,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <utility>
 #include <vector>
@@ -511,6 +512,16 @@ bool read_dataset(In &in, const char *want, int &rank, uint64_t dims[8], std::ve
     const bool f64 = esize == 8 && prec == 64 && ebits == 11 && mbits == 52;
     const bool f32 = esize == 4 && prec == 32 && ebits == 8 && mbits == 23;
     if (!f64 && !f32) return in.fail("floating-point type other than IEEE float32/float64");
+    // every stored form keeps its values inside the file: a larger dataspace
+    // is a damaged file, not an allocation to attempt
+    {
+        uint64_t c = 1;
+        for (int i = 0; i < rank; i++) {
+            if (dims[i] && c > in.size / dims[i]) return in.fail("dataspace larger than the file");
+            c *= dims[i];
+        }
+        if (c > in.size / esize) return in.fail("dataspace larger than the file");
+    }
     if (!out) return true;
     // layout
     const std::vector<uint8_t> &l = ly->data;
@@ -641,25 +652,8 @@ int ctxless(int rc, const std::string &err)
     return rc == GPSS_OK ? rc : gpss::fail(nullptr, rc, "%s", err.c_str());
 }
 
-}  // namespace
-
-extern "C" {
-
-int gpss_h5_write_field(const char *path, int ndim, const int64_t *n, const double *psi)
+int read_dataset_entry(const char *path, const char *name, int *rank, int64_t *dims, double *out, int64_t cap)
 {
-    std::string err;
-    return ctxless(write_field(path, ndim, n, psi, err), err);
-}
-
-int gpss_h5_read_field(const char *path, int ndim, const int64_t *n, double *psi)
-{
-    std::string err;
-    return ctxless(read_field(path, ndim, n, psi, err), err);
-}
-
-int gpss_h5_read_dataset(const char *path, const char *name, int *rank, int64_t *dims, double *out, int64_t cap)
-{
-    if (!path || !name || !rank || !dims) return ctxless(GPSS_EINVAL, "h5: null argument");
     In in;
     int r = 0;
     uint64_t d[8];
@@ -674,9 +668,8 @@ int gpss_h5_read_dataset(const char *path, const char *name, int *rank, int64_t 
     return GPSS_OK;
 }
 
-int gpss_write_h5(gpss_ctx *c, const char *path)
+int write_ctx(gpss_ctx *c, const char *path)
 {
-    if (!c) return GPSS_EINVAL;
     std::vector<double> psi((size_t)c->total * 2);
     const int rc = gpss_download(c, psi.data());
     if (rc != GPSS_OK) return rc;
@@ -685,14 +678,63 @@ int gpss_write_h5(gpss_ctx *c, const char *path)
     return w == GPSS_OK ? w : gpss::fail(c, w, "%s", err.c_str());
 }
 
-int gpss_read_h5(gpss_ctx *c, const char *path)
+int read_ctx(gpss_ctx *c, const char *path)
 {
-    if (!c) return GPSS_EINVAL;
     std::vector<double> psi((size_t)c->total * 2);
     std::string err;
     const int r = read_field(path, c->ndim, c->n, psi.data(), err);
     if (r != GPSS_OK) return gpss::fail(c, r, "%s", err.c_str());
     return gpss_upload(c, psi.data());
+}
+
+// No C++ exception leaves an entry point: a failed host allocation is ENOMEM.
+template <typename F> int guarded(gpss_ctx *c, F body)
+{
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        return gpss::fail(c, GPSS_ENOMEM, "h5: host allocation failed");
+    } catch (...) {
+        return gpss::fail(c, GPSS_EIO, "h5: unexpected failure");
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpss_h5_write_field(const char *path, int ndim, const int64_t *n, const double *psi)
+{
+    return guarded(nullptr, [&] {
+        std::string err;
+        return ctxless(write_field(path, ndim, n, psi, err), err);
+    });
+}
+
+int gpss_h5_read_field(const char *path, int ndim, const int64_t *n, double *psi)
+{
+    return guarded(nullptr, [&] {
+        std::string err;
+        return ctxless(read_field(path, ndim, n, psi, err), err);
+    });
+}
+
+int gpss_h5_read_dataset(const char *path, const char *name, int *rank, int64_t *dims, double *out, int64_t cap)
+{
+    if (!path || !name || !rank || !dims) return ctxless(GPSS_EINVAL, "h5: null argument");
+    return guarded(nullptr, [&] { return read_dataset_entry(path, name, rank, dims, out, cap); });
+}
+
+int gpss_write_h5(gpss_ctx *c, const char *path)
+{
+    if (!c) return GPSS_EINVAL;
+    return guarded(c, [&] { return write_ctx(c, path); });
+}
+
+int gpss_read_h5(gpss_ctx *c, const char *path)
+{
+    if (!c) return GPSS_EINVAL;
+    return guarded(c, [&] { return read_ctx(c, path); });
 }
 
 }  // extern "C"

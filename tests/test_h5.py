@@ -155,6 +155,14 @@ def test_read_errors(L, sfd, tmp_path):
     bad.write_bytes(bytes(b[:len(b) - 8]))  # truncated raw data
     with pytest.raises(_lib.GPSSError, match="out of the file"):
         sfd.read_h5_dataset(str(bad), "re")
+    # a dataspace far larger than the file is refused before any allocation
+    dims = (4).to_bytes(8, "little") + (8).to_bytes(8, "little")
+    b3 = bytearray(b)
+    at = b3.index(dims)
+    b3[at:at + 8] = (1 << 40).to_bytes(8, "little")
+    bad.write_bytes(bytes(b3))
+    with pytest.raises(_lib.GPSSError, match="larger than the file"):
+        sfd.read_h5_dataset(str(bad), "im")
 
 
 def test_reads_float32_big_endian_and_user_block(L, sfd, tmp_path):
