@@ -44,6 +44,7 @@ struct gpss_ctx {
     // entry point that may change the field or the parameters bumps version
     uint64_t version = 0, ecache_version = ~uint64_t(0);
     double ecache[5] = {0, 0, 0, 0, 0}, ecache_mass = 0;
+    int ecache_mass_slot = 0;  // sums slot holding the raw mass the cached energies came with
     int device = 0;
     cudaStream_t stream = nullptr;
     void *psi = nullptr;      // device field (float2 or double2)

@@ -157,8 +157,19 @@ template <typename T> static int imag_merged(gpss_ctx *c, int nsteps, double dt)
     return apply_scale<T>(c);
 }
 
+// the cached energies of the current field (GPSS_FLAG_ENERGY_CACHE), if any
+static bool ecache_fresh(const gpss_ctx *c)
+{
+    return (c->flags & GPSS_FLAG_ENERGY_CACHE) && c->ecache_version == c->version;
+}
+
+// mass_slot >= 0: that sums slot holds the mass of the current field (the
+// previous call measured it with the cached energies and nothing has changed
+// since), so the FP32 mass lock takes its target from there instead of a
+// read-only pass.
 template <typename T>
-static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_diag *diag)
+static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_diag *diag,
+                     int mass_slot = -1)
 {
     const bool plain = (c->flags & GPSS_FLAG_PLAIN) != 0;
     const bool merge = !plain && !imag && scheme == GPSS_STRANG && c->omega == 0.0 &&
@@ -175,6 +186,7 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         if (diag) {
             diag->steps = 0;
             GPSS_TRY(energy_impl<T>(c, diag->energy, &diag->mass));
+            c->ecache_mass_slot = 0;
         }
         return GPSS_OK;
     }
@@ -182,7 +194,15 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         int zero = 0;
         CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     }
-    if (lock) GPSS_TRY(diag_passes<T>(c, false, FIN_NONE));  // target mass -> diagnostics slot
+    if (lock) {  // target mass -> diagnostics slot
+        if (mass_slot >= 0) {
+            CUDA_TRY(c, cudaMemcpyAsync(c->sums + kDiagSlot * RQ_COUNT + RQ_MASS,
+                                        c->sums + mass_slot * RQ_COUNT + RQ_MASS, sizeof(double),
+                                        cudaMemcpyDeviceToDevice, c->stream));
+        } else {
+            GPSS_TRY(diag_passes<T>(c, false, FIN_NONE));
+        }
+    }
     if (plain) {
         for (int s = 0; s < nsteps; s++) {
             if (scheme == GPSS_STRANG) {
@@ -259,8 +279,10 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
                 return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
             energies_from_sums(c, h, last, diag->energy);
             diag->mass = times_cell(c, h[last * RQ_COUNT + RQ_MASS]);
+            c->ecache_mass_slot = last;
         } else {
             GPSS_TRY(energy_impl<T>(c, diag->energy, &diag->mass));
+            c->ecache_mass_slot = 0;  // diag_passes with the kinetic sums: the mass is in slot 0
         }
     }
     return GPSS_OK;
@@ -469,6 +491,7 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
 {
     NvtxRange nvtx_("gpss_step");
     if (!c) return GPSS_EINVAL;
+    const int mass_slot = ecache_fresh(c) ? c->ecache_mass_slot : -1;  // before the version moves on
     c->version++;  // the field or the parameters may change
     if (nsteps < 0) return fail(c, GPSS_EINVAL, "nsteps must be >= 0");
     if (scheme != GPSS_LIE && scheme != GPSS_STRANG) return fail(c, GPSS_EINVAL, "scheme must be 1 (Lie) or 2 (Strang)");
@@ -483,8 +506,8 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
     if (!d && (c->flags & GPSS_FLAG_ENERGY_CACHE) && !imag && scheme == GPSS_STRANG && c->omega == 0.0 &&
         !(c->flags & (GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE)) && nsteps > 0)
         d = &own;
-    const int rc = c->precision == GPSS_FP32 ? step_impl<float>(c, nsteps, scheme, imag, dt, d)
-                                             : step_impl<double>(c, nsteps, scheme, imag, dt, d);
+    const int rc = c->precision == GPSS_FP32 ? step_impl<float>(c, nsteps, scheme, imag, dt, d, mass_slot)
+                                             : step_impl<double>(c, nsteps, scheme, imag, dt, d, mass_slot);
     if (rc == GPSS_OK && d) {
         for (int i = 0; i < 5; i++) c->ecache[i] = d->energy[i];
         c->ecache_mass = d->mass;
@@ -493,11 +516,6 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
     return rc;
 }
 
-// the cached energies of the current field (GPSS_FLAG_ENERGY_CACHE), if any
-static bool ecache_fresh(const gpss_ctx *c)
-{
-    return (c->flags & GPSS_FLAG_ENERGY_CACHE) && c->ecache_version == c->version;
-}
 
 
 
