@@ -524,8 +524,7 @@ static double times_cell(const gpss_ctx *c, double x)
 // normalize! (Fields.jl:196-200) on the device: unit mass from the FP64 sum
 template <typename T> static int normalize_impl(gpss_ctx *c)
 {
-    int zero = 0;
-    CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
     GPSS_TRY(diag_passes<T>(c, false, FIN_UNITMASS));
     GPSS_TRY(apply_scale<T>(c));
     int st = 0;

@@ -191,8 +191,7 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         return GPSS_OK;
     }
     if (imag || lock) {
-        int zero = 0;
-        CUDA_TRY(c, cudaMemcpyAsync(c->status, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
     }
     if (lock) {  // target mass -> diagnostics slot
         if (mass_slot >= 0) {
