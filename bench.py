@@ -26,6 +26,10 @@ JSON line keys beyond the base contract:
   imag_time      cfg2: 128^3 imaginary-time steps, FP32 and FP64.
   adjoint        cfg4: one 2000-step gradient through gpss_adjoint.
   rk4            the explicit RK4 integrator (NumModelGPRK) on the cfg1 field.
+  solve          solve! iterations (energy + one step) with and without the
+                 energy cache; implicit: the BE/CN Krylov schemes (cfg2, 64^3).
+  checkpoint     one WriterSave res-<istep>.h5 of the cfg1 field written from
+                 and read back into the device field.
   cufft_comparison  the same directional pass through cuFFT (torch.fft).
 
 --impl reference times the CPU restatement of the reference path (the
@@ -69,7 +73,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the accuracy, cfg2, cfg4 and cuFFT measurements")
-    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve", "implicit"], default=None,
+    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve", "implicit", "checkpoint"], default=None,
                     help="run one secondary measurement alone and print it (profiling runs)")
     ap.add_argument("--only-steps", type=int, default=None,
                     help="with --only imag/solve: time steps (iterations) to time")
@@ -384,6 +388,36 @@ def measure_solve(sfd, c, iters=20):
     return out
 
 
+def measure_checkpoint(sfd, c):
+    """WriterSave's res-<istep>.h5 (Writers.jl:41-137) of the cfg1 field at
+    256^3 (FP32 on the device), written from the device field and read back
+    into it: seconds and GB/s of file per direction (a 268 MB file: "re" and
+    "im" as float64)."""
+    import shutil
+    import tempfile
+    grid = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(grid)
+    f.phi = c["psi"]
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+    m = sfd.NumModelSplit2(f, p, c["dt"], 1, 1, precision="fp32")
+    d = tempfile.mkdtemp(prefix="gpss_ckpt_")
+    try:
+        w = sfd.WriterSave(f)
+        prefix = os.path.join(d, "res")
+        t0 = time.perf_counter()
+        w.write(prefix=prefix, istep=0)
+        tw = time.perf_counter() - t0
+        size = os.path.getsize(prefix + "-0.h5")
+        t0 = time.perf_counter()
+        w.read(prefix=prefix, istep=0)
+        tr = time.perf_counter() - t0
+    finally:
+        m.close(download=False)
+        shutil.rmtree(d, ignore_errors=True)
+    return {"workload": "cfg1 field, 256^3 FP32 on the device, one res-<istep>.h5 (float64 re/im) to a temporary directory",
+            "file_bytes": size, "write_s": tw, "read_s": tr, "write_GBps": size / tw / 1e9, "read_GBps": size / tr / 1e9}
+
+
 def measure_implicit(sfd, W, steps=4):
     """The implicit schemes (imaginary-time BE and CN with the reference's
     BiCGStab) on the cfg2 physics at 64^3, FP64: time per step and Krylov
@@ -423,6 +457,8 @@ def run_only(args):
         r = measure_rk(sfd, W.cfg1(256), L)
     elif args.only == "implicit":
         r = measure_implicit(sfd, W)
+    elif args.only == "checkpoint":
+        r = measure_checkpoint(sfd, W.cfg1(256))
     else:
         r = measure_solve(sfd, W.cfg1(256), iters=args.only_steps or 20)
     print(json.dumps(r), flush=True)
@@ -602,6 +638,7 @@ def run_gpss(args, rank, world, local):
         extra["rk4"] = measure_rk(sfd, c, L)
         extra["solve"] = measure_solve(sfd, c)
         extra["implicit"] = measure_implicit(sfd, W)
+        extra["checkpoint"] = measure_checkpoint(sfd, c)
         cu = measure_cufft(c, args.n)
         if cu:
             cu["gpss_pass_ms"] = per_axis
