@@ -45,6 +45,9 @@ struct gpss_ctx {
     uint64_t version = 0, ecache_version = ~uint64_t(0);
     double ecache[5] = {0, 0, 0, 0, 0}, ecache_mass = 0;
     int ecache_mass_slot = 0;  // sums slot holding the raw mass the cached energies came with
+    // pinned host copy of the sums (4 slots) and the status word, so that the
+    // end of a step call reads both with one synchronisation
+    double *host_stage = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
     void *psi = nullptr;      // device field (float2 or double2)

@@ -261,18 +261,22 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
             }
         }
     }
-    if (imag || lock) {
+    // the status word and (with fused diagnostics) the sums, one synchronisation
+    const bool check = imag || lock, want_sums = diag && diag_done;
+    double *h = c->host_stage;
+    if (check) CUDA_TRY(c, cudaMemcpyAsync(h + 4 * RQ_COUNT, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (want_sums)
+        CUDA_TRY(c, cudaMemcpyAsync(h, c->sums, sizeof(double) * 4 * RQ_COUNT, cudaMemcpyDeviceToHost, c->stream));
+    if (check || want_sums) CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (check) {
         int st = 0;
-        CUDA_TRY(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        std::memcpy(&st, h + 4 * RQ_COUNT, sizeof(int));
         if (st & 2) return fail(c, GPSS_ETIMEOUT, "a pipelined pass gave up waiting for a tile copy");
         if (st) return fail(c, GPSS_ENONFINITE, "a renormalisation saw a non-finite or zero mass");
     }
     if (diag) {
         diag->steps = nsteps;
         if (diag_done) {
-            double h[4 * RQ_COUNT];
-            GPSS_TRY(read_sums(c, h));
             const int last = c->ndim - 1;
             if (!std::isfinite(h[last * RQ_COUNT + RQ_MASS]))
                 return fail(c, GPSS_ENONFINITE, "field holds NaN/Inf");
@@ -321,6 +325,7 @@ void gpss_destroy(gpss_ctx *c)
         cudaStreamDestroy(c->side);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->host_stage) cudaFreeHost(c->host_stage);
     delete c;
 }
 
@@ -404,6 +409,12 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if ((rc = dev_alloc(c, (void **)&c->scale, sizeof(double) * 2))) return bail(rc);
     if ((rc = dev_alloc(c, (void **)&c->status, sizeof(int) * 2))) return bail(rc);
     if ((rc = dev_alloc(c, (void **)&c->counter, sizeof(unsigned int) * 2))) return bail(rc);
+    e = cudaHostAlloc((void **)&c->host_stage, sizeof(double) * (4 * RQ_COUNT + 1), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        c->host_stage = nullptr;
+        fail(c, GPSS_ENOMEM, "cudaHostAlloc: %s", cudaGetErrorString(e));
+        return bail(GPSS_ENOMEM);
+    }
     e = cudaMemset(c->counter, 0, sizeof(unsigned int) * 2);
     if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemset: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }
     const ScaleCell one = {1.0, 1.0f};
