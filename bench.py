@@ -4,9 +4,15 @@
 Workload (cfg1): 3D real-time GP, Strang splitting (NumModelSplit2), 256^3
 periodic box [0, 2pi]^3, V = 0, coeffD = -xi/sqrt(2), beta = 1/(sqrt(2) xi),
 xi = 0.05, psi0 = e^{i theta} with 64 seeded Fourier modes; dt = 2.5e-3.
-One bench step = one cfg1 run of 200 time steps through gpss_step (FP32 fused
-kernels, FP64 reductions) from the cfg1 initial field, which is restored in
-HBM (outside the timed events) before every bench step.
+One bench step = one cfg1 run of 200 time steps through gpss_step from the
+cfg1 initial field, which is restored in HBM (outside the timed events)
+before every bench step.  The timed form is the FP32 one that meets the
+metric's accuracy bar (rel-L2 <= 1e-5 against the FP64 oracle after 200
+steps): FP32 storage with compensated (double-float) arithmetic in the fused
+passes (GPSS_FLAG_COMPENSATED), FP64 reductions.  The plain FP32 passes are
+timed beside it (`fp32_plain`): they are 4x faster but reach 2.5e-5 at step
+200, because the Strang step is resonant on the |k| ~ 188 shell of this grid
+(|coeffD| |k|^2 dt = pi) and amplifies their rounding.
 
 Metric: Mcell-steps/s = cells x time steps / seconds.  The field (134 MB FP32)
 is larger than L2 and every pass streams 268 MB, so no L2 flush is needed.
@@ -22,7 +28,10 @@ JSON line keys beyond the base contract:
   fp64_plain     the FP64 plain kernels (reference stage order) on the same
                  workload, the comparison the headline metric names.
   batched        cfg3: 512 mixed-size 2D runs in one persistent launch.
-  accuracy       rel-L2 of the FP32 fused field vs the FP64 plain field.
+  fp32_plain     the plain FP32 fused passes on the same workload (value,
+                 per-pass times, roofline).
+  accuracy       rel-L2 of the FP32 fields (compensated and plain) and of the
+                 FP64 fused field against the FP64 oracle after 50..200 steps.
   imag_time      cfg2: 128^3 imaginary-time steps, FP32 and FP64.
   adjoint        cfg4: one 2000-step gradient through gpss_adjoint.
   rk4            the explicit RK4 integrator (NumModelGPRK) on the cfg1 field.
@@ -33,7 +42,10 @@ JSON line keys beyond the base contract:
   cufft_comparison  the same directional pass through cuFFT (torch.fft).
 
 --impl reference times the CPU restatement of the reference path (the
-reference itself is Julia + FFTW, which does not exist on this machine).
+reference itself is Julia + FFTW, which does not exist on this machine): the
+time-step loop of the FP64 C oracle on all host cores, grid and plan setup
+excluded (the reference's own benchmark times timeStep! alone), plus a
+labelled scipy.fft (pocketfft, threaded) restatement as an FFTW-class leg.
 """
 from __future__ import annotations
 
@@ -67,16 +79,20 @@ def parse():
     ap.add_argument("--n", type=int, default=CELLS_N, help="grid points per axis (default 256)")
     ap.add_argument("--timesteps", type=int, default=TIMESTEPS_PER_STEP,
                     help="time steps per bench step (default 200, the cfg1 run length)")
+    ap.add_argument("--kernels", default="compensated", choices=["compensated", "plain"],
+                    help="FP32 form timed as the headline (default: compensated, the one that meets 1e-5)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the accuracy, cfg2, cfg4 and cuFFT measurements")
-    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve", "implicit", "checkpoint"], default=None,
+    ap.add_argument("--only", choices=["imag", "adjoint", "batch", "rk4", "solve", "implicit", "checkpoint", "passes"],
+                    default=None,
                     help="run one secondary measurement alone and print it (profiling runs)")
     ap.add_argument("--only-steps", type=int, default=None,
-                    help="with --only imag/solve: time steps (iterations) to time")
+                    help="with --only imag/solve: time steps (iterations) to time; with --only passes: "
+                         "launches per axis")
     return ap.parse_args()
 
 
@@ -193,16 +209,15 @@ def oracle_mod():
     return gp_oracle
 
 
-def cpu_sample(c, O, timesteps=1, nthreads=0):
-    """One bounded sample of the workload on the CPU oracle; returns (cell-steps/s, cores)."""
+def cpu_sample(c, O, timesteps=1, nthreads=0, psi=None):
+    """One bounded sample of the workload on the CPU oracle, timing its
+    time-step loop alone; returns (cell-steps/s, cores, seconds, field)."""
     cores = nthreads or os.cpu_count() or 1
-    psi = c["psi"]
-    t0 = time.perf_counter()
-    O.c_step(psi, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"], nsteps=timesteps,
-             dt=c["dt"], nthreads=cores)
-    dt = time.perf_counter() - t0
+    psi = c["psi"] if psi is None else psi
+    out, dt = O.c_step_timed(psi, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], V=c["V"],
+                             nsteps=timesteps, dt=c["dt"], nthreads=cores)
     cells = float(math.prod(c["shape"]))
-    return cells * timesteps / dt, cores, dt
+    return cells * timesteps / dt, cores, dt, out
 
 
 METRIC = "GP split-step Mcell-steps/s at 256^3: FP32 fused vs FP64 plain @ relL2<=1e-5"
@@ -223,15 +238,26 @@ def run_reference(args, rank, world):
     c = W.cfg1(args.n)
     O = oracle_mod()
     cores = os.cpu_count() or 1
+    psi = c["psi"]
     for _ in range(args.warmup):
-        cpu_sample(c, O, 1, cores)
-    vals, secs = [], 0.0
-    for _ in range(args.steps):
-        v, _, dt = cpu_sample(c, O, 1, cores)
-        vals.append(v)
+        _, _, _, psi = cpu_sample(c, O, 1, cores, psi)
+    secs = 0.0
+    for _ in range(args.steps):  # timeStep! after timeStep!, the loop alone timed
+        _, _, dt, psi = cpu_sample(c, O, 1, cores, psi)
         secs += dt
     value = (float(math.prod(c["shape"])) * args.steps) / secs / 1e6
-    sample = f"1 Strang time step of cfg1 at {args.n}^3 per bench step (FP64, own radix-2 FFT, OpenMP)"
+    sample = (f"1 Strang time step of cfg1 at {args.n}^3 per bench step, continuing the run (FP64, own "
+              "radix-2 FFT, OpenMP); the step loop is timed, grid/plan/field setup is not")
+    # FFTW-class leg: the same steps with scipy.fft (pocketfft, threaded)
+    sp_steps = 2
+    _, sp_s = O.sp_step_timed(c["psi"], c["bounds"], coeffD=c["coeffD"], beta=c["beta"], nsteps=1,
+                              dt=c["dt"], workers=cores)
+    _, sp_s = O.sp_step_timed(c["psi"], c["bounds"], coeffD=c["coeffD"], beta=c["beta"], nsteps=sp_steps,
+                              dt=c["dt"], workers=cores)
+    scipy_leg = {"value": float(math.prod(c["shape"])) * sp_steps / sp_s / 1e6, "unit": "Mcell-steps/s",
+                 "cores": cores, "kind": "port",
+                 "sample": f"{sp_steps} Strang time steps of cfg1 at {args.n}^3: scipy.fft (pocketfft) "
+                           f"threaded over {cores} workers, numpy broadcasts single-threaded"}
     line = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -244,6 +270,7 @@ def run_reference(args, rank, world):
         "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "scipy_fft_leg": scipy_leg,
         "note": "CPU restatement of NumModelSplit2 (oracle/gp_oracle.c); the reference's Julia/FFTW "
                 "runtime is not installed on this machine",
     }
@@ -275,30 +302,37 @@ def measure_batch(sfd, W, calls=3):
             "max_rel_mass_drift": float(np.max(np.abs(m - m0) / m0))}
 
 
-def _model(sfd, c, precision, form="fused", V=None, steps=1):
+def _model(sfd, c, precision, form="fused", V=None, steps=1, compensated=False):
     grid = sfd.Grid(c["shape"], c["bounds"])
     f = sfd.Field(grid)
     f.phi = c["psi"]
     pot = sfd.PotentialZero(f) if V is None else sfd.PotentialArray(f, V)
     p = sfd.GrossPitaevskiiParameters(pot, coeffD=c["coeffD"], beta=c["beta"])
-    return f, sfd.NumModelSplit2(f, p, c["dt"], steps, steps, precision=precision, form=form)
+    return f, sfd.NumModelSplit2(f, p, c["dt"], steps, steps, precision=precision, form=form,
+                                 compensated=compensated)
 
 
-def measure_accuracy(sfd, c, marks=(50, 100, 150, 200)):
-    """rel-L2 of the FP32 fused field against the FP64 plain field (the FP64
-    kernels match the oracle to 1e-13 in the tests) after each mark."""
-    f32, m32 = _model(sfd, c, "fp32")
-    f64, m64 = _model(sfd, c, "fp64", "plain")
-    out, done = {}, 0
+def measure_accuracy(sfd, c, O, marks=(50, 100, 150, 200)):
+    """rel-L2 against the FP64 oracle (oracle/gp_oracle.c run live on the host
+    cores, about 40 s for 200 steps at 256^3) after each mark, for the FP32
+    compensated form (the headline), the plain FP32 passes and the FP64 fused
+    merged form."""
+    forms = {"fp32_compensated": dict(precision="fp32", compensated=True),
+             "fp32_plain": dict(precision="fp32"),
+             "fp64_fused": dict(precision="fp64")}
+    models = {k: _model(sfd, c, **kw) for k, kw in forms.items()}
+    out = {k: {} for k in forms}
+    ref, done = c["psi"], 0
     for k in marks:
-        m32.step(k - done)
-        m64.step(k - done)
+        ref = O.c_step(ref, c["bounds"], coeffD=c["coeffD"], beta=c["beta"], nsteps=k - done, dt=c["dt"])
+        for name, (f, m) in models.items():
+            m.step(k - done)
+            out[name][str(k)] = O.rel_l2(f.phi, ref)
         done = k
-        a, b = f32.phi, f64.phi
-        out[str(k)] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    m32.close(download=False)
-    m64.close(download=False)
-    return {"rel_l2_fp32_fused_vs_fp64_plain": out, "bar": 1e-5}
+    for f, m in models.values():
+        m.close(download=False)
+    return {"rel_l2_vs_fp64_oracle": out, "bar": 1e-5, "bar_met_at_200": {
+        k: v[str(marks[-1])] <= 1e-5 for k, v in out.items()}}
 
 
 def _event_ms(L, h, fn):
@@ -385,6 +419,26 @@ def measure_solve(sfd, c, iters=20):
         t = time.perf_counter() - t0
         m.close(download=False)
         out["cache" if cache else "no_cache"] = {"ms_per_iteration": t / iters * 1e3}
+    # a timeStep! loop without energies: one-step calls chain through the
+    # pending half kinetic flow (one flow per call), flushed at the end
+    grid = sfd.Grid(c["shape"], c["bounds"])
+    f = sfd.Field(grid)
+    f.phi = c["psi"]
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
+    m = sfd.NumModelSplit2(f, p, c["dt"], iters, iters, precision="fp32")
+    from sfd_gb300 import _lib
+    L = _lib.lib()
+    for _ in range(3):
+        sfd.timeStep(m)
+    L.gpss_sync(m.handle)
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        sfd.timeStep(m)
+    L.gpss_sync(m.handle)
+    t = time.perf_counter() - t0
+    m.close(download=False)
+    out["timestep_loop"] = {"ms_per_call": t / iters * 1e3,
+                            "note": "timeStep! called once per step, no energy in between (host-timed, sync at the end)"}
     return out
 
 
@@ -439,6 +493,23 @@ def measure_implicit(sfd, W, steps=4):
     return out
 
 
+def measure_passes(sfd, c, L, compensated, reps=20):
+    """Each fused directional pass of the cfg1 merged step alone (x, y, z with
+    the nonlinear epilogue), `reps` launches per axis after one warm-up, CUDA
+    events (the command behind the per-pass ncu captures in profiles/)."""
+    f, m = _model(sfd, c, "fp32", compensated=compensated)
+    out = {"workload": f"cfg1 field, {c['shape'][0]}^3, FP32 {'compensated' if compensated else 'plain'} "
+                       f"fused passes, {reps} launches per axis"}
+    for axis in range(3):
+        ms = ctypes.c_double()
+        rc = L.gpss_time_pass(m.handle, axis, 1 if axis == 2 else 0, reps, c["dt"], ctypes.byref(ms))
+        if rc != 0:
+            raise RuntimeError(L.gpss_last_error(m.handle).decode())
+        out["xyz"[axis] + "_ms"] = ms.value
+    m.close(download=False)
+    return out
+
+
 def run_only(args):
     """One secondary measurement alone (for profiling it), one JSON line."""
     import importlib
@@ -459,6 +530,8 @@ def run_only(args):
         r = measure_implicit(sfd, W)
     elif args.only == "checkpoint":
         r = measure_checkpoint(sfd, W.cfg1(256))
+    elif args.only == "passes":
+        r = measure_passes(sfd, W.cfg1(args.n), L, args.kernels == "compensated", reps=args.only_steps or 20)
     else:
         r = measure_solve(sfd, W.cfg1(256), iters=args.only_steps or 20)
     print(json.dumps(r), flush=True)
@@ -519,7 +592,8 @@ def run_gpss(args, rank, world, local):
     f = sfd.Field(grid)
     f.phi = c["psi"]
     p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
-    model = sfd.NumModelSplit2(f, p, c["dt"], nt, nt, precision="fp32")
+    comp = args.kernels == "compensated"
+    model = sfd.NumModelSplit2(f, p, c["dt"], nt, nt, precision="fp32", compensated=comp)
     h = model.handle
     ck = lambda rc: _lib.check(rc, h)
 
@@ -537,6 +611,7 @@ def run_gpss(args, rank, world, local):
     for _ in range(args.warmup):
         restore()
         ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+        ck(L.gpss_flush(h))
     ck(L.gpss_sync(h))
     dist.barrier()
     clocks = ClockSampler(local)
@@ -550,6 +625,7 @@ def run_gpss(args, rank, world, local):
         l0 = L.gpss_launch_count(h)
         ck(L.gpss_event_record(h, 0))
         ck(L.gpss_step(h, nt, 2, 0, c["dt"], None))
+        ck(L.gpss_flush(h))  # the call's last half kinetic flow, inside the timed region
         ck(L.gpss_event_record(h, 1))
         ck(L.gpss_event_elapsed(h, 0, 1, ctypes.byref(ms)))
         launches += L.gpss_launch_count(h) - l0
@@ -561,21 +637,37 @@ def run_gpss(args, rank, world, local):
     restore()
 
     # ---- dominant kernel timing (roofline): each fused pass alone, CUDA events
-    per_axis = {}
-    for axis in range(3):
-        out = ctypes.c_double()
-        ck(L.gpss_time_pass(h, axis, 1 if axis == 2 else 0, 20, c["dt"], ctypes.byref(out)))
-        per_axis["xyz"[axis]] = out.value
-    dom = max(per_axis, key=per_axis.get)
-    dom_ms = per_axis[dom]
     alg_bytes = BYTES_PER_CELL_PASS * cells
     peak, peak_kind = measured_hbm_peak()
-    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
-    tag = f"pass_fp32_{dom}_cfg1_{args.n}"
-    traffic = profiled_traffic(tag)
-    # whole-step bandwidth: 3 passes per merged step plus the final half step per call
-    passes_per_call = PASSES_PER_TIMESTEP * (nt + 1)
-    step_gbs = BYTES_PER_CELL_PASS * cells * passes_per_call * args.steps / (t_ms / 1e3) / 1e9
+    passes_per_call = PASSES_PER_TIMESTEP * (nt + 1)  # 3 per merged step + the final half step
+
+    def pass_times(hh):
+        per = {}
+        for axis in range(3):
+            out = ctypes.c_double()
+            _lib.check(L.gpss_time_pass(hh, axis, 1 if axis == 2 else 0, 20, c["dt"], ctypes.byref(out)), hh)
+            per["xyz"[axis]] = out.value
+        return per
+
+    def roofline(per, tagform, ms_step):
+        dom = max(per, key=per.get)
+        achieved = alg_bytes / (per[dom] / 1e3) / 1e9
+        step_gbs = BYTES_PER_CELL_PASS * cells * passes_per_call / (ms_step / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profiled_traffic(f"pass_{tagform}_{dom}_cfg1_{args.n}"), "kernel": f"fused {dom} pass",
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": per,
+                "whole_step_gbs": step_gbs, "whole_step_frac": step_gbs / peak,
+                "whole_step_bytes_per_cell_step": BYTES_PER_CELL_PASS * PASSES_PER_TIMESTEP,
+                "note": "per-pass frac: 16 B/cell per launch (one read and one write of the FP32 field); "
+                        "whole step: the 3 merged passes per time step (48 B/cell-step)"}
+
+    per_axis = pass_times(h)
+    roof = roofline(per_axis, "fp32c" if comp else "fp32", t_ms / args.steps)
+    if comp:
+        roof["note"] += ("; the compensated passes are bound by the FP32 pipe (double-float arithmetic, "
+                         "see profiles/), not by HBM")
 
     # ---- end to end through the public API with host buffers
     nbytes = int(cells) * 16
@@ -604,6 +696,33 @@ def run_gpss(args, rank, world, local):
         _lib.check(L.gpss_host_free(hbuf))
     model.close(download=False)
 
+    # ---- the other FP32 form on the same workload (the plain passes when the
+    # compensated ones are the headline)
+    other = None
+    if not args.no_extra:
+        f2 = sfd.Field(grid)
+        f2.phi = c["psi"]
+        p2 = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f2), coeffD=c["coeffD"], beta=c["beta"])
+        m2 = sfd.NumModelSplit2(f2, p2, c["dt"], nt, nt, precision="fp32", compensated=not comp)
+        h2 = m2.handle
+        k2 = 5
+        t2 = 0.0
+        for i in range(k2 + 2):
+            _lib.check(L.gpss_upload(h2, p0), h2)
+            _lib.check(L.gpss_sync(h2), h2)
+            _lib.check(L.gpss_event_record(h2, 0), h2)
+            _lib.check(L.gpss_step(h2, nt, 2, 0, c["dt"], None), h2)
+            _lib.check(L.gpss_flush(h2), h2)
+            _lib.check(L.gpss_event_record(h2, 1), h2)
+            _lib.check(L.gpss_event_elapsed(h2, 0, 1, ctypes.byref(ms)), h2)
+            if i >= 2:
+                t2 += ms.value
+        per2 = pass_times(h2)
+        m2.close(download=False)
+        other = {"form": "compensated" if not comp else "plain", "value": cells * nt * k2 / (t2 / 1e3) / 1e6,
+                 "unit": "Mcell-steps/s", "ms_per_step": t2 / k2, "steps": k2,
+                 "roofline": roofline(per2, "fp32" if comp else "fp32c", t2 / k2)}
+
     # ---- FP64 plain kernels on the same workload (fewer time steps)
     fp64 = None
     if not args.no_fp64:
@@ -622,7 +741,9 @@ def run_gpss(args, rank, world, local):
         m64.close(download=False)
         v64 = cells * k64 / (ms64.value / 1e3) / 1e6
         fp64 = {"value": v64, "unit": "Mcell-steps/s", "timesteps": k64,
-                "ms_per_timestep": ms64.value / k64, "fp32_fused_over_fp64_plain": value / world / v64}
+                "ms_per_timestep": ms64.value / k64, "fp32_over_fp64_plain": value / world / v64}
+        if other:
+            other["fp32_over_fp64_plain"] = other["value"] / v64
 
     # ---- batched runs (cfg3)
     batch = None
@@ -632,7 +753,7 @@ def run_gpss(args, rank, world, local):
     # ---- accuracy, imaginary time (cfg2), adjoint (cfg4), cuFFT comparison
     extra = {}
     if not args.no_extra and rank == 0 and args.n == 256:
-        extra["accuracy"] = measure_accuracy(sfd, c)
+        extra["accuracy"] = measure_accuracy(sfd, c, oracle_mod())
         extra["imag_time"] = measure_imag(sfd, W, L)
         extra["adjoint"] = measure_adjoint(sfd, W)
         extra["rk4"] = measure_rk(sfd, c, L)
@@ -648,13 +769,13 @@ def run_gpss(args, rank, world, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         O = oracle_mod()
-        v, cores, dt = cpu_sample(c, O, 1, os.cpu_count() or 1)
+        v, cores, dt, _ = cpu_sample(c, O, 1, os.cpu_count() or 1)
         steps = max(1, min(128, int(12.0 / max(dt, 1e-3))))  # about 12 s of CPU work
         if steps > 1:
-            v, cores, dt = cpu_sample(c, O, steps, os.cpu_count() or 1)
+            v, cores, dt, _ = cpu_sample(c, O, steps, os.cpu_count() or 1)
         cpu = {"value": v / 1e6, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
                "sample": f"{steps} Strang time step(s) of cfg1 at {args.n}^3 on the FP64 C oracle "
-                         f"(own radix-2 FFT, OpenMP), {dt:.1f} s"}
+                         f"(own radix-2 FFT, OpenMP), step loop {dt:.1f} s (setup not timed)"}
 
     dist.close()
     if rank != 0:
@@ -666,7 +787,8 @@ def run_gpss(args, rank, world, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded cfg1 phase field, 64 modes |k|<=4)",
         "config": {"workload": workload_name(args.n),
-                   "kernels": "FP32 fused",
+                   "kernels": ("FP32 fused, compensated (double-float arithmetic, FP32 storage)" if comp
+                               else "FP32 fused, plain"),
                    "grid": [args.n] * 3, "timesteps_per_step": nt,
                    "l2": "inputs larger than L2 (134 MB field, 268 MB streamed per pass); no flush",
                    "initial_field": "restored before every bench step (outside the timed events)",
@@ -674,15 +796,10 @@ def run_gpss(args, rank, world, local):
         "gpu_launches": int(launches),
         "e2e": None if e2e is None else {"value": e2e, "unit": "Mcell-steps/s", "h2d_bytes_per_step": nbytes,
                                          "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": f"fused {dom} pass",
-                     "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
-                     else "fallback 6800 GB/s",
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "ms_per_launch": per_axis,
-                     "whole_step_gbs": step_gbs},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "fp64_plain": fp64,
+        ("fp32_plain" if comp else "fp32_compensated"): other,
         "batched": batch,
     }
     line.update(extra)

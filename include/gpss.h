@@ -2,7 +2,7 @@
  * gpss.h -- C ABI of libgpss.so, the GB300 split-step Gross-Pitaevskii
  * library.  It replaces the time-stepping hot path of SuperfluidDynamics.jl
  * (NumModelSplit1 / NumModelSplit2 on a periodic Grid) behind plain C types so
- * that Julia can bind it with ccall (see INTEGRATION.md).
+ * that Julia can bind it with ccall.
  *
  * Conventions
  *   - Fields are column-major with x fastest and complex values interleaved
@@ -47,13 +47,21 @@ extern "C" {
 #define GPSS_FLAG_PIPE 8      /* x passes through the persistent asynchronous-copy
                                  pipeline (same arithmetic; the direct kernel is
                                  faster on GB300 and is the default) */
-#define GPSS_FLAG_ENERGY_CACHE 16 /* real-time Strang with Omega = 0 (fused, merged):
-                                 every gpss_step also measures the energies of its
-                                 final field in its last passes, and gpss_energy /
+#define GPSS_FLAG_ENERGY_CACHE 16 /* real-time Strang (fused forms): every
+                                 gpss_step also measures the energies of its
+                                 final field in its last passes (with Omega != 0
+                                 plus one read-only x pass), and gpss_energy /
                                  gpss_mass return them while the field and the
                                  parameters are unchanged -- so solve!'s energy
                                  then timeStep! (NumModels.jl:33-35) costs no
-                                 read-only passes */
+                                 read-only passes, or one with rotation */
+#define GPSS_FLAG_COMPENSATED 32 /* FP32 fields: the fused kinetic passes of the
+                                 split steps run their transforms, twiddles and
+                                 phase on double-float (hi + lo) FP32 values, so
+                                 the only FP32 rounding of a pass is the store
+                                 of the field (about 3x the instructions of a
+                                 plain FP32 pass); the merged imaginary-time
+                                 step keeps its plain FP32 passes */
 
 /* split schemes of gpss_step */
 #define GPSS_LIE 1            /* NumModelSplit1: L(dt) N(dt) */
@@ -110,6 +118,14 @@ int gpss_download(gpss_ctx *ctx, double *psi);
  * mass after every step (an extension; the reference has no imaginary-time
  * split step).  diag may be NULL; when given, it receives the mass and
  * energies of the final field.
+ * A real-time Strang call with Omega = 0 (fused forms) runs the merged
+ * sequence L(dt/2) N [L(dt) N]^(nsteps-1) and, unless diag is given, leaves
+ * its last half kinetic flow L(dt/2) pending: the next such call folds it into
+ * its first flow (so a loop of one-step calls costs one kinetic flow per
+ * step), and every entry point that reads or changes the field -- download,
+ * energy, mass, norm, normalize, set_params, set_potential, the other
+ * integrators, sync, flush -- applies it first.  Results are bitwise those of
+ * the eager sequence.
  */
 int gpss_step(gpss_ctx *ctx, int nsteps, int scheme, int imag, double dt, gpss_diag *diag);
 
@@ -255,11 +271,20 @@ int gpss_select_device(int device);
 /* Number of CUDA devices visible to the library (0 when there is none). */
 int gpss_device_count(void);
 
-/* Block the host until the context's stream is idle. */
+/* Block the host until the context's stream is idle (after applying a
+ * pending half kinetic flow, see gpss_step). */
 int gpss_sync(gpss_ctx *ctx);
 
 /* Record CUDA event `slot` (0..7) on the context's stream. */
 int gpss_event_record(gpss_ctx *ctx, int slot);
+
+/*
+ * Apply now the half kinetic flow that a merged real-time Strang call of
+ * gpss_step leaves pending (see gpss_step).  Every entry point that reads or
+ * changes the field does this itself; call it to end a timed region with the
+ * field complete.  No counterpart in the reference (its timeStep! is eager).
+ */
+int gpss_flush(gpss_ctx *ctx);
 
 /* Milliseconds between two recorded events (synchronises on `b`). */
 int gpss_event_elapsed(gpss_ctx *ctx, int a, int b, float *ms);
@@ -299,8 +324,10 @@ int64_t gpss_device_bytes(const gpss_ctx *ctx);
  * that loads it until the process exits.  Fields whose largest reduction
  * needs more partial sums than fit are rejected with GPSS_EINVAL (256^3 fits).
  * The first call on a device looks that array up; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race, so
- * serialise them.  Returns 0 or a negative GPSS_E* code (no message).
+ * capture.  The address is kept for the life of the process: a
+ * cudaDeviceReset between calls is not supported.  Calls share the array:
+ * calls that overlap on the GPU race, so serialise them.  Returns 0 or a
+ * negative GPSS_E* code; the message is available from gpss_last_error(NULL).
  */
 int gpss_energy_noalloc(int ndim, const int64_t *n, const double *lo, const double *hi, int precision,
                         double coeffD, double beta, double omega, const void *psi_dev, const void *V_dev,

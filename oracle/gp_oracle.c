@@ -460,9 +460,9 @@ int OR_SYM(or_fft_axis)(int ndim, const int64_t *n, double *psi, int axis, int i
  * imag != 0: imaginary time with unit-mass renormalisation after each step.
  * V may be NULL (PotentialZero).  nthreads <= 0 keeps the OpenMP default.
  */
-int OR_SYM(or_step)(int ndim, const int64_t *n, const double *lo, const double *hi,
-                    double cD, double beta, double Om, const double *V, double *psi,
-                    int nsteps, int scheme, int imag, double dt, int nthreads)
+static int step_impl(int ndim, const int64_t *n, const double *lo, const double *hi,
+                     double cD, double beta, double Om, const double *V, double *psi,
+                     int nsteps, int scheme, int imag, double dt, int nthreads, double *loop_seconds)
 {
     ogrid g;
     if (scheme != 1 && scheme != 2) return -1;
@@ -478,6 +478,9 @@ int OR_SYM(or_step)(int ndim, const int64_t *n, const double *lo, const double *
 #endif
     /* Julia: n.Δt * 0.5 is a Float64 product, then used as the step */
     const real rdt = (real)dt, half = (real)(dt * 0.5);
+#ifdef _OPENMP
+    const double t0 = omp_get_wtime();
+#endif
     for (int s = 0; s < nsteps; s++) {
         if (scheme == 2) {
             solve_lap_rot(&g, p, (real)cD, (real)Om, half, imag);
@@ -495,12 +498,32 @@ int OR_SYM(or_step)(int ndim, const int64_t *n, const double *lo, const double *
         }
     }
 #ifdef _OPENMP
+    if (loop_seconds) *loop_seconds = omp_get_wtime() - t0;
     omp_set_num_threads(saved);
+#else
+    if (loop_seconds) *loop_seconds = -1.0;
 #endif
     store_field(p, psi, g.total);
     free(p); free(Vr);
     grid_free(&g);
     return 0;
+}
+
+int OR_SYM(or_step)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                    double cD, double beta, double Om, const double *V, double *psi,
+                    int nsteps, int scheme, int imag, double dt, int nthreads)
+{
+    return step_impl(ndim, n, lo, hi, cD, beta, Om, V, psi, nsteps, scheme, imag, dt, nthreads, NULL);
+}
+
+/* or_step that also reports the wall time of the time-step loop alone (grid,
+ * plans and field conversion excluded), the part the reference's own
+ * benchmark times (benchmarks/scalability_gp.jl:40-51 times timeStep! only). */
+int OR_SYM(or_step_timed)(int ndim, const int64_t *n, const double *lo, const double *hi,
+                          double cD, double beta, double Om, const double *V, double *psi,
+                          int nsteps, int scheme, int imag, double dt, int nthreads, double *loop_seconds)
+{
+    return step_impl(ndim, n, lo, hi, cD, beta, Om, V, psi, nsteps, scheme, imag, dt, nthreads, loop_seconds);
 }
 
 /*

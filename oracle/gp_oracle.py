@@ -57,6 +57,8 @@ class _Bound:
         self.or_step.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        self.or_step_timed = g("or_step_timed")
+        self.or_step_timed.argtypes = self.or_step.argtypes + [_f64p]
         self.or_derivatives = g("or_derivatives")
         self.or_derivatives.argtypes = [ctypes.c_int, _i64p, _f64p, _f64p, _f64p] + [_f64p] * 8
         self.or_energy = g("or_energy")
@@ -171,6 +173,23 @@ def c_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, s
     if rc != 0:
         raise ValueError("or_step failed")
     return out
+
+
+def c_step_timed(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, scheme=2,
+                 imag=False, dt=1e-3, nthreads=0):
+    """c_step that also returns the seconds of the time-step loop alone (setup
+    of grid, plans and field excluded): (field, seconds)."""
+    out = _field(psi).copy(order="F")
+    nd, n, lo, hi = _geom(out.shape, bounds)
+    Vp = None if V is None else np.asfortranarray(V, dtype=np.float64)
+    secs = ctypes.c_double(-1.0)
+    L = lib()
+    rc = L.or_step_timed(nd, n.ctypes.data_as(_i64p), _p(lo), _p(hi), coeffD, beta, omega, _p(Vp),
+                         _p(out), int(nsteps), int(scheme), 1 if imag else 0, float(dt), int(nthreads),
+                         ctypes.cast(ctypes.byref(secs), _f64p))
+    if rc != 0:
+        raise ValueError("or_step_timed failed")
+    return out, secs.value
 
 
 RK_STEPPERS = {"RK1": 1, "RK2": 2, "RK4": 4}
@@ -461,6 +480,36 @@ def np_step(psi, bounds, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, nsteps=1, 
             nrm = np.sqrt(np.sum(np.abs(p) ** 2)) * np.sqrt(np.prod(d))
             p /= nrm
     return p
+
+
+def sp_step_timed(psi, bounds, *, coeffD=-0.5, beta=1.0, V=None, nsteps=1, dt=1e-3, workers=0):
+    """Strang steps (scheme 2, real time, Omega = 0) with scipy.fft (pocketfft,
+    threaded over `workers`) as the transform and numpy broadcasts (single
+    threaded, like the reference's Julia broadcasts) for the phase and
+    nonlinear stages: an FFTW-class CPU restatement for timing.  Returns
+    (field, seconds of the step loop)."""
+    import time
+    import scipy.fft as sfft
+    workers = workers or os.cpu_count() or 1
+    p = np.array(psi, dtype=np.complex128, order="F", copy=True)
+    nd = p.ndim
+    d = spacing(p.shape, bounds)
+    facs = []
+    for a in range(nd):
+        xi = fftfreq(p.shape[a], d[a])
+        s = [1] * nd
+        s[a] = xi.size
+        facs.append(np.exp(1j * ((coeffD * (xi * xi)) * (dt * 0.5))).reshape(s))
+    Vv = None if V is None else np.asarray(V, dtype=np.float64)
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        for half in range(2):
+            for a in range(nd):
+                p = sfft.ifft(facs[a] * sfft.fft(p, axis=a, workers=workers), axis=a, workers=workers)
+            if half == 0:
+                r = (0.0 if Vv is None else Vv) + beta * (p.real ** 2 + p.imag ** 2)
+                p = np.exp(1j * (-r * dt)) * p
+    return p, time.perf_counter() - t0
 
 
 def rel_l2(a, b) -> float:

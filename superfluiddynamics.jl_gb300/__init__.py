@@ -34,8 +34,8 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_ENERGY_CACHE, GPSS_FLAG_NOMASSLOCK,
-                   GPSS_FLAG_NOMERGE, GPSS_FLAG_PIPE, GPSS_FLAG_PLAIN)
+from ._lib import (GPSSError, GPSS_FP32, GPSS_FP64, GPSS_FLAG_COMPENSATED, GPSS_FLAG_ENERGY_CACHE,
+                   GPSS_FLAG_NOMASSLOCK, GPSS_FLAG_NOMERGE, GPSS_FLAG_PIPE, GPSS_FLAG_PLAIN)
 
 __all__ = ["Grid", "Field", "norm", "normalize", "GrossPitaevskiiParameters", "PotentialZero",
            "PotentialQuadratic", "NumModelSplit1", "NumModelSplit2", "timeStep", "energy",
@@ -208,7 +208,7 @@ class _SplitModel:
 
     def __init__(self, f: Field, param: GrossPitaevskiiParameters, dt, niter, freqbckp, *,
                  precision="fp64", form="fused", merge=True, masslock=True, pipeline=False,
-                 energy_cache=False, writers=()):
+                 energy_cache=False, compensated=False, writers=()):
         if f._owner is not None:
             raise ValueError("this field already belongs to a model")
         if form not in ("fused", "plain"):
@@ -230,7 +230,8 @@ class _SplitModel:
         hi = (ctypes.c_double * 3)(*(list(g.max) + [1.0] * (3 - nd)))
         flags = ((GPSS_FLAG_PLAIN if form == "plain" else 0) | (0 if merge else GPSS_FLAG_NOMERGE)
                  | (0 if masslock else GPSS_FLAG_NOMASSLOCK) | (GPSS_FLAG_PIPE if pipeline else 0)
-                 | (GPSS_FLAG_ENERGY_CACHE if energy_cache else 0))
+                 | (GPSS_FLAG_ENERGY_CACHE if energy_cache else 0)
+                 | (GPSS_FLAG_COMPENSATED if compensated else 0))
         h = ctypes.c_void_p()
         _lib.check(L.gpss_create(ctypes.byref(h), nd, n, lo, hi, _PRECISION[precision], flags))
         self._h = h

@@ -29,6 +29,7 @@ GPSS_FLAG_NOMERGE = 2
 GPSS_FLAG_NOMASSLOCK = 4
 GPSS_FLAG_PIPE = 8
 GPSS_FLAG_ENERGY_CACHE = 16
+GPSS_FLAG_COMPENSATED = 32
 GPSS_LIE = 1
 GPSS_STRANG = 2
 
@@ -94,6 +95,7 @@ SIGNATURES = {
     "gpss_batch_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]),
     "gpss_sync": (ctypes.c_int, [_vp]),
+    "gpss_flush": (ctypes.c_int, [_vp]),
     "gpss_event_record": (ctypes.c_int, [_vp, ctypes.c_int]),
     "gpss_event_elapsed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_float)]),

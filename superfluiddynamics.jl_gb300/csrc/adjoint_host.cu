@@ -292,6 +292,7 @@ int gpss_adjoint(gpss_ctx *c, const double *psi_target, int nsteps, int K, doubl
     if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "dt must be finite");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     if (c->precision == GPSS_FP32) return adjoint_impl<float>(c, psi_target, nsteps, K, dt, loss, dLdV, dLdpsi0);
     return adjoint_impl<double>(c, psi_target, nsteps, K, dt, loss, dLdV, dLdpsi0);
 }

@@ -448,41 +448,10 @@ static int bfail(gpss_batch *b, int code, const char *fmt, ...)
 
 typedef long double ldouble;
 
-static void root_of_unity(int64_t k, int64_t n, ldouble *cs, ldouble *sn)
-{
-    const ldouble half_pi = 1.570796326794896619231321691639751442L;
-    k %= n;
-    if (k < 0) k += n;
-    const int64_t q = (4 * k) / n, r4 = 4 * k - q * n;
-    ldouble cc, ss;
-    if (2 * r4 <= n) {
-        const ldouble a = half_pi * (ldouble)r4 / (ldouble)n;
-        cc = cosl(a); ss = sinl(a);
-    } else {
-        const ldouble a = half_pi * (ldouble)(n - r4) / (ldouble)n;
-        cc = sinl(a); ss = cosl(a);
-    }
-    switch (q) {
-    case 0: *cs = cc; *sn = ss; break;
-    case 1: *cs = -ss; *sn = cc; break;
-    case 2: *cs = -cc; *sn = -ss; break;
-    default: *cs = ss; *sn = -cc; break;
-    }
-}
-
 // float2 hi[m] / lo[m] pairs from long-double values, rows of n
 static std::vector<float2> dw_table(const std::vector<ldouble> &re, const std::vector<ldouble> &im, int64_t n)
 {
-    const int64_t rows = (int64_t)re.size() / n;
-    std::vector<float2> out((size_t)(2 * n * rows));
-    for (int64_t r = 0; r < rows; r++)
-        for (int64_t k = 0; k < n; k++) {
-            const size_t i = (size_t)(r * n + k);
-            const float hr = (float)re[i], hi = (float)im[i];
-            out[(size_t)(r * 2 * n + k)] = make_float2(hr, hi);
-            out[(size_t)(r * 2 * n + n + k)] = make_float2((float)(re[i] - (ldouble)hr), (float)(im[i] - (ldouble)hi));
-        }
-    return out;
+    return dw_split<float>(re, im, n);
 }
 
 static int upload(gpss_batch *b, const std::vector<float2> &h, const float2 **dev)
@@ -505,17 +474,8 @@ static int build_tables(gpss_batch *b, double dt)
     std::vector<TableSet> sets(b->set_keys.size());
     for (size_t si = 0; si < b->set_keys.size(); si++) {
         const int64_t n = b->set_keys[si].first;
-        const int64_t N1 = n <= 16 ? n : 16, N2 = n / N1;
-        std::vector<ldouble> re((size_t)(2 * n)), im((size_t)(2 * n));
-        for (int64_t k1 = 0; k1 < N1; k1++)
-            for (int64_t r = 0; r < N2; r++) {
-                ldouble cs, sn;
-                root_of_unity(r * k1, n, &cs, &sn);
-                re[(size_t)(k1 * N2 + r)] = cs;
-                im[(size_t)(k1 * N2 + r)] = -sn;
-                re[(size_t)(n + r * N1 + k1)] = cs;
-                im[(size_t)(n + r * N1 + k1)] = -sn;
-            }
+        std::vector<ldouble> re, im;
+        twiddle_rows(n, re, im);
         int rc = upload(b, dw_table(re, im, n), &sets[si].tw);
         if (rc) return rc;
         for (int axis = 0; axis < 2; axis++) {

@@ -43,6 +43,11 @@ struct gpss_ctx {
     // energies of the field as of `version` (GPSS_FLAG_ENERGY_CACHE); every
     // entry point that may change the field or the parameters bumps version
     uint64_t version = 0, ecache_version = ~uint64_t(0);
+    // a merged real-time Strang call leaves its trailing half kinetic flow
+    // L(pending_h) unapplied (see flush_pending); pending_scale: the mass
+    // lock's factor in `scale` is still to be applied by that flow's first pass
+    double pending_h = 0.0;
+    bool pending_scale = false;
     double ecache[5] = {0, 0, 0, 0, 0}, ecache_mass = 0;
     int ecache_mass_slot = 0;  // sums slot holding the raw mass the cached energies came with
     // pinned host copy of the sums (4 slots) and the status word, so that the
@@ -115,31 +120,6 @@ struct NvtxRange {
 };
 
 typedef long double ldouble;
-static const ldouble kHalfPiL = 1.570796326794896619231321691639751442L;
-
-// (cos, sin) of 2 pi k / n in long double, reduced to the first octant so
-// that the symmetric values are exact.
-static void unit_root(int64_t k, int64_t n, ldouble *cs, ldouble *sn)
-{
-    k %= n;
-    if (k < 0) k += n;
-    int64_t q = (4 * k) / n;
-    int64_t r4 = 4 * k - q * n;
-    ldouble cc, ss;
-    if (2 * r4 <= n) {
-        ldouble a = kHalfPiL * (ldouble)r4 / (ldouble)n;
-        cc = cosl(a); ss = sinl(a);
-    } else {
-        ldouble a = kHalfPiL * (ldouble)(n - r4) / (ldouble)n;
-        cc = sinl(a); ss = cosl(a);
-    }
-    switch (q) {
-    case 0: *cs = cc; *sn = ss; break;
-    case 1: *cs = -ss; *sn = cc; break;
-    case 2: *cs = -cc; *sn = -ss; break;
-    default: *cs = ss; *sn = -cc; break;
-    }
-}
 
 // Grids.jl:78-84: x = LinRange(lo, hi, n+1)[1:end-1] (lerps of Base.LinRange)
 static double lerpi(int64_t j, int64_t dd, double a, double b)
@@ -173,35 +153,16 @@ static size_t real_bytes(const gpss_ctx *c) { return c->precision == GPSS_FP32 ?
 static int upload_dw(gpss_ctx *c, void **dev, const std::vector<ldouble> &re, const std::vector<ldouble> &im,
                      int64_t rows, int64_t n)
 {
-    std::vector<double> h((size_t)(4 * n * rows));  // re/im pairs of hi and lo as doubles
-    std::vector<ldouble> lo_re(re.size()), lo_im(im.size());
+    (void)rows;
     if (c->precision == GPSS_FP32) {
-        std::vector<float> f((size_t)(4 * n * rows));
-        for (int64_t r = 0; r < rows; r++)
-            for (int64_t k = 0; k < n; k++) {
-                const size_t i = (size_t)(r * n + k);
-                const float hr = (float)re[i], hi = (float)im[i];
-                const float lr = (float)(re[i] - (ldouble)hr), li = (float)(im[i] - (ldouble)hi);
-                f[(size_t)(2 * (r * 2 * n + k))] = hr;
-                f[(size_t)(2 * (r * 2 * n + k) + 1)] = hi;
-                f[(size_t)(2 * (r * 2 * n + n + k))] = lr;
-                f[(size_t)(2 * (r * 2 * n + n + k) + 1)] = li;
-            }
-        GPSS_TRY(dev_alloc(c, dev, f.size() * 4));
-        CUDA_TRY(c, cudaMemcpy(*dev, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+        const std::vector<float2> f = dw_split<float>(re, im, n);
+        GPSS_TRY(dev_alloc(c, dev, f.size() * sizeof(float2)));
+        CUDA_TRY(c, cudaMemcpy(*dev, f.data(), f.size() * sizeof(float2), cudaMemcpyHostToDevice));
         return GPSS_OK;
     }
-    for (int64_t r = 0; r < rows; r++)
-        for (int64_t k = 0; k < n; k++) {
-            const size_t i = (size_t)(r * n + k);
-            const double hr = (double)re[i], hi = (double)im[i];
-            h[(size_t)(2 * (r * 2 * n + k))] = hr;
-            h[(size_t)(2 * (r * 2 * n + k) + 1)] = hi;
-            h[(size_t)(2 * (r * 2 * n + n + k))] = (double)(re[i] - (ldouble)hr);
-            h[(size_t)(2 * (r * 2 * n + n + k) + 1)] = (double)(im[i] - (ldouble)hi);
-        }
-    GPSS_TRY(dev_alloc(c, dev, h.size() * 8));
-    CUDA_TRY(c, cudaMemcpy(*dev, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
+    const std::vector<double2> h = dw_split<double>(re, im, n);
+    GPSS_TRY(dev_alloc(c, dev, h.size() * sizeof(double2)));
+    CUDA_TRY(c, cudaMemcpy(*dev, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
     return GPSS_OK;
 }
 
@@ -382,11 +343,27 @@ static bool pipe_ok(const gpss_ctx *c, int axis)
     return true;
 }
 
+// Host-side fault injection for tests: GPSS_FAULT_PIPE_POLLS=v in the
+// environment makes the pipelined pass poll a tile's barrier only v times
+// before it gives up (0: at once), so the bounded-wait path -- status 2,
+// GPSS_ETIMEOUT, the CTA draining its own copies -- runs without any GPU fault.
+static unsigned injected_pipe_polls()
+{
+    const char *v = std::getenv("GPSS_FAULT_PIPE_POLLS");
+    if (!v || !*v) return 0u;
+    return (unsigned)std::strtoul(v, nullptr, 10) + 1u;
+}
+
 template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const PassArgs<T> &a)
 {
-    if (mode == MODE_FUSED && !a.acc && !a.nl_pre && !a.dot_with && pipe_ok(c, axis)) {
+    if (mode == MODE_FUSED && !a.acc && !a.nl_pre && !a.dot_with && !a.comp && pipe_ok(c, axis)) {
         const int ntiles = (int)(c->total / c->n[axis] / (4096 / c->n[axis]));
-        cudaError_t e = PassLauncher<T>::pipe(axis == 0, (int)c->n[axis], a, ntiles, c->stream);
+        PassArgs<T> ap = a;
+        ap.wait_polls = injected_pipe_polls();
+        // a wait that gives up is recorded in the status word even when the
+        // pass has no reduction of its own (the x pass of a step)
+        if (!ap.fin_status) ap.fin_status = c->status;
+        cudaError_t e = PassLauncher<T>::pipe(axis == 0, (int)c->n[axis], ap, ntiles, c->stream);
         if (e != cudaSuccess)
             return fail(c, GPSS_ECUDA, "pipelined pass launch (axis %d): %s", axis, cudaGetErrorString(e));
         c->launches++;
@@ -435,6 +412,7 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
         const void *ph;
         GPSS_TRY(get_phase(c, axis, dtl, imag, 1, &ph, &a.prow));
         a.phase = (const vec2<T> *)ph;
+        a.comp = sizeof(T) == 4 && (c->flags & GPSS_FLAG_COMPENSATED) != 0;
         if (prescale && step == 0) a.scale = c->scale;
         const bool last = step == c->ndim - 1;
         if (last && nl) {
@@ -454,6 +432,36 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
         GPSS_TRY(launch<T>(c, axis, MODE_FUSED, a));
     }
     return GPSS_OK;
+}
+
+// A merged real-time Strang call (Omega = 0, fused) ends with
+// L(dt/2) N, leaving its trailing half kinetic flow L(dt/2) unapplied: the
+// device holds phi with psi = L(pending_h) phi.  The next such call folds it
+// into its first flow (L(a) L(b) = L(a + b) when the flows commute), so a
+// loop of one-step calls runs the merged sequence; every other entry point
+// that reads or changes the field applies it first (flush_pending), or drops
+// it when it replaces the field.  The flow is the same table and launch
+// sequence as the trailing half step would have been, so results are
+// bitwise those of the eager sequence.
+template <typename T> static int flush_pending_t(gpss_ctx *c)
+{
+    if (c->pending_h == 0.0) return GPSS_OK;
+    const double h = c->pending_h;
+    const bool ps = c->pending_scale;
+    c->pending_h = 0.0;
+    c->pending_scale = false;
+    return kinetic_fused<T>(c, h, 0, false, 0.0, 0, false, ps);
+}
+static int flush_pending(gpss_ctx *c)
+{
+    if (c->pending_h == 0.0) return GPSS_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    return c->precision == GPSS_FP32 ? flush_pending_t<float>(c) : flush_pending_t<double>(c);
+}
+static void drop_pending(gpss_ctx *c)
+{
+    c->pending_h = 0.0;
+    c->pending_scale = false;
 }
 
 // Plain form: per axis FFT -> multiply -> iFFT as three launches
@@ -500,6 +508,17 @@ template <typename T> static int diag_passes(gpss_ctx *c, bool kin, int mode)
         GPSS_TRY(launch<T>(c, axis, MODE_DIAG, a));
     }
     return GPSS_OK;
+}
+
+// Parseval kinetic sums of one axis of the current field (read-only pass) into
+// sums slot `axis`
+template <typename T> static int diag_kin_axis(gpss_ctx *c, int axis)
+{
+    PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
+    a.red = RED_KIN;
+    a.coord = axis == 0 ? c->coord_dev[1] : (axis == 1 ? c->coord_dev[0] : nullptr);
+    set_finish<T>(c, a, axis, FIN_NONE);
+    return launch<T>(c, axis, MODE_DIAG, a);
 }
 
 template <typename T> static int apply_scale(gpss_ctx *c)

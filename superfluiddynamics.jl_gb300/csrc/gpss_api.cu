@@ -182,6 +182,10 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
     const int red_nl = lock ? RED_MASS : 0;
     const int fin_nl = lock ? FIN_MASSLOCK : FIN_NONE;
     bool diag_done = false;
+    // continue the previous call's merged sequence (its pending half flow is
+    // folded into this call's first flow), or apply that flow first
+    const bool chain = merge && nsteps > 0 && c->pending_h != 0.0;
+    if (!chain) GPSS_TRY(flush_pending_t<T>(c));
     if (nsteps == 0) {
         if (diag) {
             diag->steps = 0;
@@ -190,10 +194,13 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         }
         return GPSS_OK;
     }
-    if (imag || lock) {
+    // the status word: renormalisations and the mass lock report a non-finite
+    // mass there, the pipelined pass a wait that gave up
+    const bool pipe = (c->flags & GPSS_FLAG_PIPE) != 0;
+    if (imag || lock || pipe) {
         CUDA_TRY(c, cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
     }
-    if (lock) {  // target mass -> diagnostics slot
+    if (lock && !chain) {  // target mass -> diagnostics slot (a chained call keeps the previous target)
         if (mass_slot >= 0) {
             CUDA_TRY(c, cudaMemcpyAsync(c->sums + kDiagSlot * RQ_COUNT + RQ_MASS,
                                         c->sums + mass_slot * RQ_COUNT + RQ_MASS, sizeof(double),
@@ -219,8 +226,12 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         }
     } else if (merge) {
         // L(dt/2) N [L(dt) N]^(nsteps-1) L(dt/2): the kinetic flows of
-        // consecutive steps commute (Omega = 0) and compose exactly.
-        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, red_nl, false, false, fin_nl));
+        // consecutive steps commute (Omega = 0) and compose exactly.  A
+        // pending flow of the previous call joins the first one.
+        const double lead = dt * 0.5 + c->pending_h;
+        const bool lead_scale = c->pending_scale;
+        drop_pending(c);
+        GPSS_TRY(kinetic_fused<T>(c, lead, 0, true, dt, red_nl, false, lead_scale, fin_nl));
         int s = 1;
         if (c->total <= kGraphCells) {
             const std::string key = graph_key("step", {dt, (double)lock, (double)kGraphChunk});
@@ -235,9 +246,15 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
             GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, red_nl, false, lock, fin_nl));
         // final half step; with diag, the kinetic sums of each axis are exact
         // for the final field (real-time kinetic flows are unitary and commute
-        // with the other axes' derivatives when Omega = 0)
-        GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, diag ? RED_POINT : 0, diag != nullptr, lock));
-        diag_done = diag != nullptr;
+        // with the other axes' derivatives when Omega = 0).  Without diag it
+        // is left pending for the next call or the next read of the field.
+        if (diag) {
+            GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, RED_POINT, true, lock));
+            diag_done = true;
+        } else {
+            c->pending_h = dt * 0.5;
+            c->pending_scale = lock;
+        }
     } else if (imag && scheme == GPSS_STRANG && c->omega == 0.0 && !(c->flags & GPSS_FLAG_NOMERGE)) {
         GPSS_TRY(imag_merged<T>(c, nsteps, dt));
     } else if (imag) {
@@ -255,14 +272,26 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
         for (int s = 0; s < nsteps; s++) {
             if (scheme == GPSS_STRANG) {
                 GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, true, dt, red_nl, false, false, fin_nl));
-                GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, 0, false, lock));
+                if (diag && s == nsteps - 1) {
+                    // the last half step measures the energies of the final
+                    // field: its pointwise sums (last pass) and the kinetic
+                    // sums of every axis the later passes leave unchanged --
+                    // all of them when Omega = 0; with rotation the y flow
+                    // (phase x xi_y) changes the x spectrum, so the x sums come
+                    // from one read-only pass over the final field
+                    GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, RED_POINT, true, lock));
+                    if (c->omega != 0.0 && c->ndim >= 2) GPSS_TRY(diag_kin_axis<T>(c, 0));
+                    diag_done = true;
+                } else {
+                    GPSS_TRY(kinetic_fused<T>(c, dt * 0.5, 0, false, 0.0, 0, false, lock));
+                }
             } else {
                 GPSS_TRY(kinetic_fused<T>(c, dt, 0, true, dt, red_nl, false, lock && s > 0, fin_nl));
             }
         }
     }
     // the status word and (with fused diagnostics) the sums, one synchronisation
-    const bool check = imag || lock, want_sums = diag && diag_done;
+    const bool check = imag || lock || pipe, want_sums = diag && diag_done;
     double *h = c->host_stage;
     if (check) CUDA_TRY(c, cudaMemcpyAsync(h + 4 * RQ_COUNT, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     if (want_sums)
@@ -338,7 +367,8 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if (ndim != 2 && ndim != 3) return fail(nullptr, GPSS_EINVAL, "ndim must be 2 or 3 (got %d)", ndim);
     if (precision != GPSS_FP64 && precision != GPSS_FP32)
         return fail(nullptr, GPSS_EINVAL, "precision must be GPSS_FP64 or GPSS_FP32 (got %d)", precision);
-    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_PIPE | GPSS_FLAG_ENERGY_CACHE))
+    if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_PIPE | GPSS_FLAG_ENERGY_CACHE |
+                  GPSS_FLAG_COMPENSATED))
         return fail(nullptr, GPSS_EINVAL, "unknown flags 0x%x", flags);
     for (int a = 0; a < ndim; a++) {
         if (!is_pow2(n[a]) || n[a] < 2 || n[a] > 256)
@@ -381,18 +411,9 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     // twiddles per axis, stage-A layout m = k1*N2 + r: exp(-2 pi i r k1 / n) as hi + lo
     for (int a = 0; a < ndim; a++) {
         const int64_t na = c->n[a];
-        const int64_t N1 = na <= 16 ? na : 16, N2 = na / N1;
         // two rows: stage-A order (k1*N2 + r) and stage-B order (r*N1 + k1)
-        std::vector<ldouble> re((size_t)(2 * na)), im((size_t)(2 * na));
-        for (int64_t k1 = 0; k1 < N1; k1++)
-            for (int64_t r = 0; r < N2; r++) {
-                ldouble cs, sn;
-                unit_root(r * k1, na, &cs, &sn);
-                re[(size_t)(k1 * N2 + r)] = cs;
-                im[(size_t)(k1 * N2 + r)] = -sn;
-                re[(size_t)(na + r * N1 + k1)] = cs;
-                im[(size_t)(na + r * N1 + k1)] = -sn;
-            }
+        std::vector<ldouble> re, im;
+        twiddle_rows(na, re, im);
         if ((rc = upload_dw(c, &c->tw[a], re, im, 2, na))) return bail(rc);
         if ((rc = dev_alloc(c, (void **)&c->coord_dev[a], sizeof(double) * (size_t)c->n[a]))) return bail(rc);
         e = cudaMemcpy(c->coord_dev[a], c->coord[a].data(), sizeof(double) * (size_t)c->n[a], cudaMemcpyHostToDevice);
@@ -431,6 +452,7 @@ int gpss_set_params(gpss_ctx *c, double coeffD, double beta, double omega)
     if (!std::isfinite(coeffD) || !std::isfinite(beta) || !std::isfinite(omega))
         return fail(c, GPSS_EINVAL, "parameters must be finite");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));  // with the parameters it was computed for
     if (coeffD != c->cD || omega != c->omega) clear_phases(c);
     clear_graphs(c);
     c->cD = coeffD;
@@ -444,6 +466,7 @@ int gpss_set_potential(gpss_ctx *c, const double *V)
     if (!c) return GPSS_EINVAL;
     c->version++;  // the field or the parameters may change
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     clear_graphs(c);
     if (!V) { c->have_V = false; return GPSS_OK; }
     if (!c->V) GPSS_TRY(dev_alloc(c, &c->V, (size_t)c->total * real_bytes(c)));
@@ -467,6 +490,7 @@ int gpss_upload(gpss_ctx *c, const double *psi)
     c->version++;  // the field or the parameters may change
     if (!psi) return fail(c, GPSS_EINVAL, "gpss_upload: null psi");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    drop_pending(c);  // the field is replaced
     if (c->precision == GPSS_FP64) {
         CUDA_TRY(c, cudaMemcpyAsync(c->psi, psi, (size_t)c->total * 16, cudaMemcpyHostToDevice, c->stream));
     } else {
@@ -486,6 +510,7 @@ int gpss_download(gpss_ctx *c, double *psi)
     if (!psi) return fail(c, GPSS_EINVAL, "gpss_download: null psi");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     if (c->precision == GPSS_FP64) {
         CUDA_TRY(c, cudaMemcpyAsync(psi, c->psi, (size_t)c->total * 16, cudaMemcpyDeviceToHost, c->stream));
     } else {
@@ -513,8 +538,8 @@ int gpss_step(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, gpss_dia
     // at no extra sweep (merged real-time Strang), do so and keep them
     gpss_diag own;
     gpss_diag *d = diag;
-    if (!d && (c->flags & GPSS_FLAG_ENERGY_CACHE) && !imag && scheme == GPSS_STRANG && c->omega == 0.0 &&
-        !(c->flags & (GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE)) && nsteps > 0)
+    if (!d && (c->flags & GPSS_FLAG_ENERGY_CACHE) && !imag && scheme == GPSS_STRANG &&
+        !(c->flags & GPSS_FLAG_PLAIN) && nsteps > 0)
         d = &own;
     const int rc = c->precision == GPSS_FP32 ? step_impl<float>(c, nsteps, scheme, imag, dt, d, mass_slot)
                                              : step_impl<double>(c, nsteps, scheme, imag, dt, d, mass_slot);
@@ -539,6 +564,7 @@ int gpss_energy(gpss_ctx *c, double *out)
         return GPSS_OK;
     }
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     if (c->precision == GPSS_FP32) return energy_impl<float>(c, out, nullptr);
     return energy_impl<double>(c, out, nullptr);
 }
@@ -548,6 +574,7 @@ static int raw_mass(gpss_ctx *c, double *out)
 {
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     int rc = c->precision == GPSS_FP32 ? diag_passes<float>(c, false, FIN_NONE)
                                        : diag_passes<double>(c, false, FIN_NONE);
     if (rc) return rc;
@@ -589,6 +616,7 @@ int gpss_normalize(gpss_ctx *c)
     c->version++;  // the field or the parameters may change
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     return c->precision == GPSS_FP32 ? normalize_impl<float>(c) : normalize_impl<double>(c);
 }
 
@@ -640,8 +668,15 @@ int gpss_sync(gpss_ctx *c)
 {
     if (!c) return GPSS_EINVAL;
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return GPSS_OK;
+}
+
+int gpss_flush(gpss_ctx *c)
+{
+    if (!c) return GPSS_EINVAL;
+    return flush_pending(c);
 }
 
 int gpss_event_record(gpss_ctx *c, int slot)
@@ -676,12 +711,14 @@ int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double 
         return fail(c, GPSS_EINVAL, "time_pass: bad axis/mode/reps");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     auto run = [&](auto tag) -> int {
         using T = decltype(tag);
         PassArgs<T> a = axis_args<T>(c, axis, c->psi, c->psi);
         const void *ph;
         GPSS_TRY(get_phase(c, axis, dt, 0, 1, &ph, &a.prow));
         a.phase = (const vec2<T> *)ph;
+        a.comp = sizeof(T) == 4 && (c->flags & GPSS_FLAG_COMPENSATED) != 0;
         if (mode == 1) {
             a.nl_mode = NL_REAL;
             a.V = c->have_V ? (const T *)c->V : nullptr;

@@ -1,12 +1,80 @@
 // gpss_internal.h -- declarations shared by the translation units of libgpss.
 #pragma once
 #include <cuda_runtime.h>
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
 #include "pass_kernel.cuh"
 
 namespace gpss {
+
+// ---- host-side tables shared by the context, the batch and the no-alloc path
+
+// (cos, sin) of 2 pi k / n in long double, reduced to the first octant so
+// that the symmetric values are exact.
+inline void unit_root(int64_t k, int64_t n, long double *cs, long double *sn)
+{
+    const long double half_pi = 1.570796326794896619231321691639751442L;
+    k %= n;
+    if (k < 0) k += n;
+    const int64_t q = (4 * k) / n, r4 = 4 * k - q * n;
+    long double cc, ss;
+    if (2 * r4 <= n) {
+        const long double a = half_pi * (long double)r4 / (long double)n;
+        cc = cosl(a); ss = sinl(a);
+    } else {
+        const long double a = half_pi * (long double)(n - r4) / (long double)n;
+        cc = sinl(a); ss = cosl(a);
+    }
+    switch (q) {
+    case 0: *cs = cc; *sn = ss; break;
+    case 1: *cs = -ss; *sn = cc; break;
+    case 2: *cs = -cc; *sn = -ss; break;
+    default: *cs = ss; *sn = -cc; break;
+    }
+}
+
+// The twiddles w_n^{r k1} = exp(-2 pi i r k1 / n) of a line of n cells in the
+// pass kernel's two orders: row 0 at m = k1*N2 + r (stage A), row 1 at
+// m = r*N1 + k1 (stage B), N1 = min(n, 16), N2 = n / N1.
+inline void twiddle_rows(int64_t n, std::vector<long double> &re, std::vector<long double> &im)
+{
+    const int64_t N1 = n <= 16 ? n : 16, N2 = n / N1;
+    re.assign((size_t)(2 * n), 0.0L);
+    im.assign((size_t)(2 * n), 0.0L);
+    for (int64_t k1 = 0; k1 < N1; k1++)
+        for (int64_t r = 0; r < N2; r++) {
+            long double cs, sn;
+            unit_root(r * k1, n, &cs, &sn);
+            re[(size_t)(k1 * N2 + r)] = cs;
+            im[(size_t)(k1 * N2 + r)] = -sn;
+            re[(size_t)(n + r * N1 + k1)] = cs;
+            im[(size_t)(n + r * N1 + k1)] = -sn;
+        }
+}
+
+// Complex values in rows of n (long double) as double-word pairs of the field
+// precision: per row hi[n] then lo[n], hi + lo = value.
+template <typename T>
+std::vector<vec2<T>> dw_split(const std::vector<long double> &re, const std::vector<long double> &im, int64_t n)
+{
+    const int64_t rows = (int64_t)re.size() / n;
+    std::vector<vec2<T>> out((size_t)(2 * n * rows));
+    for (int64_t r = 0; r < rows; r++)
+        for (int64_t k = 0; k < n; k++) {
+            const size_t i = (size_t)(r * n + k);
+            const T hr = (T)re[i], hi = (T)im[i];
+            vec2<T> h, l;
+            h.x = hr;
+            h.y = hi;
+            l.x = (T)(re[i] - (long double)hr);
+            l.y = (T)(im[i] - (long double)hi);
+            out[(size_t)(r * 2 * n + k)] = h;
+            out[(size_t)(r * 2 * n + n + k)] = l;
+        }
+    return out;
+}
 
 // pass launchers (pass_f32.cu / pass_f64.cu)
 cudaError_t launch_pass_f32(int mode, bool xl, int n, const PassArgs<float> &a, int blocks,

@@ -20,7 +20,10 @@
 // address: the first call on each device looks the address up with
 // cudaGetSymbolAddress (with that device current) and every launch passes the
 // looked-up pointer.  That first call should therefore come before any stream
-// capture.  Every call shares the array and leaves its contents behind; the
+// capture.  The looked-up address is kept for the life of the process, so a
+// cudaDeviceReset between calls (which unloads the library's device code and
+// with it the array) is not supported.  Every call shares the array and leaves
+// its contents behind; the
 // arrival counter is cleared by each call before its kernels run.  Calls whose
 // work overlaps on the GPU (other streams, other host threads) race on the
 // array: serialise them.
@@ -47,64 +50,42 @@ constexpr size_t kOffTw = kOffCoord + 3 * 256 * sizeof(double);    // 3 x 4 x 25
 constexpr size_t kOffPartials = kOffTw + 3 * 4 * 256 * 16;         // RQ_COUNT x CTAs doubles
 constexpr size_t kPartialBytes = GPSS_NOALLOC_SCRATCH_BYTES - kOffPartials;
 
+// The largest field the entry point takes (256^3) has at most 256^2 / W
+// tiles in one pass, W the lines of a CTA (fewest for the FP64 passes: 4), so
+// its partial sums need 16384 x 5 doubles = 640 KiB of the 969.5 KiB region
+// (1.5x margin).  The run-time check below therefore never rejects a field of
+// lines up to 256; it guards the limit should the CTA shapes change.
+static_assert((uint64_t)(256 * 256 / PassShape<double, 256, true>::W) * RQ_COUNT * sizeof(double) <=
+                  kPartialBytes, "the partial sums of a 256^3 FP64 field must fit the scratch array");
+static_assert((uint64_t)(256 * 256 / PassShape<double, 256, false>::W) * RQ_COUNT * sizeof(double) <=
+                  kPartialBytes, "the partial sums of a 256^3 FP64 field must fit the scratch array");
+
 std::mutex g_setup_mutex;
 unsigned char *g_scratch_dev[64] = {nullptr};  // looked-up device address, per device
 
-// This entry point has no context to hold a message: it reports the GPSS_E*
-// code only (the message names the failing step for readers of this file).
-int noalloc_fail(int code, const char *msg, cudaError_t e = cudaSuccess)
-{
-    (void)msg;
-    (void)e;
-    return code;
+}  // namespace
+
+namespace gpss {
+int fail(gpss_ctx *c, int code, const char *fmt, ...);  // gpss_api.cu: the message of gpss_last_error
 }
 
-typedef long double ldouble;
+namespace {
 
-// (cos, sin) of 2 pi k / n in long double, first-octant reduction
-void root_of_unity(int64_t k, int64_t n, ldouble *cs, ldouble *sn)
+// No context holds the message of this entry point: it goes where
+// gpss_last_error(NULL) reads it, as for a failed gpss_create.
+int noalloc_fail(int code, const char *msg, cudaError_t e = cudaSuccess)
 {
-    const ldouble half_pi = 1.570796326794896619231321691639751442L;
-    k %= n;
-    if (k < 0) k += n;
-    const int64_t q = (4 * k) / n, r4 = 4 * k - q * n;
-    ldouble cc, ss;
-    if (2 * r4 <= n) {
-        const ldouble a = half_pi * (ldouble)r4 / (ldouble)n;
-        cc = cosl(a); ss = sinl(a);
-    } else {
-        const ldouble a = half_pi * (ldouble)(n - r4) / (ldouble)n;
-        cc = sinl(a); ss = cosl(a);
-    }
-    switch (q) {
-    case 0: *cs = cc; *sn = ss; break;
-    case 1: *cs = -ss; *sn = cc; break;
-    case 2: *cs = -cc; *sn = -ss; break;
-    default: *cs = ss; *sn = -cc; break;
-    }
+    if (e != cudaSuccess) return gpss::fail(nullptr, code, "gpss_energy_noalloc: %s: %s", msg, cudaGetErrorString(e));
+    return gpss::fail(nullptr, code, "gpss_energy_noalloc: %s", msg);
 }
 
 // twiddle tables of one axis in the pass kernel's layout (stage A hi, lo;
-// stage B hi, lo), as interleaved reals of type T
-template <typename T> std::vector<T> twiddle_table(int64_t n)
+// stage B hi, lo)
+template <typename T> std::vector<vec2<T>> twiddle_table(int64_t n)
 {
-    const int64_t N1 = n <= 16 ? n : 16, N2 = n / N1;
-    std::vector<T> h((size_t)(8 * n));
-    auto put = [&](int64_t slot, ldouble re, ldouble im) {
-        const T hr = (T)re, hi = (T)im;
-        h[(size_t)(2 * slot)] = hr;
-        h[(size_t)(2 * slot + 1)] = hi;
-        h[(size_t)(2 * (slot + n))] = (T)(re - (ldouble)hr);
-        h[(size_t)(2 * (slot + n) + 1)] = (T)(im - (ldouble)hi);
-    };
-    for (int64_t k1 = 0; k1 < N1; k1++)
-        for (int64_t r = 0; r < N2; r++) {
-            ldouble cs, sn;
-            root_of_unity(r * k1, n, &cs, &sn);
-            put(k1 * N2 + r, cs, -sn);           // stage A order (first 2n slots)
-            put(2 * n + r * N1 + k1, cs, -sn);   // stage B order (next 2n slots)
-        }
-    return h;
+    std::vector<long double> re, im;
+    twiddle_rows(n, re, im);
+    return dw_split<T>(re, im, n);
 }
 
 double lerp_node(int64_t j, int64_t d, double a, double b)
@@ -137,8 +118,8 @@ int energy_noalloc_t(int ndim, const int64_t *n3, const double *lo, const double
         e = cudaMemcpyAsync(coord + 256 * a, x.data(), sizeof(double) * (size_t)n3[a], cudaMemcpyHostToDevice,
                             stream);
         if (e != cudaSuccess) return noalloc_fail(GPSS_ECUDA, "cudaMemcpyAsync (coordinates)", e);
-        const std::vector<T> t = twiddle_table<T>(n3[a]);
-        e = cudaMemcpyAsync(tw + (size_t)a * 4 * 256 * sizeof(vec2<T>), t.data(), sizeof(T) * t.size(),
+        const std::vector<vec2<T>> t = twiddle_table<T>(n3[a]);
+        e = cudaMemcpyAsync(tw + (size_t)a * 4 * 256 * sizeof(vec2<T>), t.data(), sizeof(vec2<T>) * t.size(),
                             cudaMemcpyHostToDevice, stream);
         if (e != cudaSuccess) return noalloc_fail(GPSS_ECUDA, "cudaMemcpyAsync (twiddles)", e);
     }

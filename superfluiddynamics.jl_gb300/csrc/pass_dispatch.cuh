@@ -72,9 +72,29 @@ static cudaError_t launch_pass_inst(const PassArgs<T> &a, int tiles, cudaStream_
     return cudaLaunchKernelEx(&cfg, k, a);
 }
 
+// compensated FP32 fused passes (FEAT_COMP), instantiated in pass_f32c*.cu
+cudaError_t launch_comp_f32(bool xl, int n, const PassArgs<float> &a, int blocks, cudaStream_t s);
+
+template <int N, bool XL>
+static cudaError_t launch_comp_mode(const PassArgs<float> &a, int blocks, cudaStream_t s)
+{
+    // the split-step kinetic passes only: phase, prescale, NL epilogue, sums
+    if (a.mask_lim || a.acc || a.pre_out || a.adj_pre || a.nl_pre || a.dot_with || a.plane_nl ||
+        a.plane_scale || !a.phase)
+        return cudaErrorInvalidValue;
+    const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0;
+    const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
+    if (diag) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_ALL>(a, blocks, s);
+    if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_NL>(a, blocks, s);
+    return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP>(a, blocks, s);
+}
+
 template <typename T, int N, bool XL>
 static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, cudaStream_t s)
 {
+    if constexpr (sizeof(T) == 4) {
+        if (mode == MODE_FUSED && a.comp) return launch_comp_f32(XL, N, a, blocks, s);
+    }
     switch (mode) {
     case MODE_FUSED: {
         // the leanest instantiation that does everything the arguments ask for
@@ -222,5 +242,13 @@ template <typename T, int N> static int lines_per_cta_n(bool xl)
         default: return 0;                                                                     \
         }                                                                                      \
     }
+
+#define GPSS_DEFINE_COMP_N(N)                                                                    \
+    cudaError_t launch_comp_f32_##N(bool xl, const PassArgs<float> &a, int blocks, cudaStream_t s) \
+    {                                                                                          \
+        return xl ? launch_comp_mode<N, true>(a, blocks, s) : launch_comp_mode<N, false>(a, blocks, s); \
+    }
+#define GPSS_DECLARE_COMP_N(N)                                                                   \
+    cudaError_t launch_comp_f32_##N(bool xl, const PassArgs<float> &a, int blocks, cudaStream_t s);
 
 }  // namespace gpss

@@ -44,6 +44,7 @@
 #pragma once
 #include <cstdint>
 #include "fft_core.cuh"
+#include "fft_comp.cuh"
 #include "nl_phase.cuh"
 
 namespace gpss {
@@ -87,8 +88,12 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //              the modes with |kk| <= mask_lim[line] (scaled by 1/n), zero the rest
 //   FEAT_ACC   the `acc` epilogue alone (add the result to a second field:
 //              the y/z passes of lapRot in the RK and implicit schemes)
+//   FEAT_COMP  (FP32) compensated arithmetic: the transforms, twiddles and
+//              phase run on double-float values (fft_comp.cuh), so the only
+//              FP32 rounding of the pass is the store; combined with
+//              FEAT_NONE, FEAT_NL or FEAT_ALL
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
-       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128 };
+       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128, FEAT_COMP = 256 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -171,6 +176,11 @@ template <typename T> struct PassArgs {
     const vec2<T> *dot_with;
     // FEAT_MASK: the largest kept |kk| of each line (-1: none)
     const int *mask_lim;
+    // FP32 FUSED passes: nonzero selects the compensated instantiation (FEAT_COMP)
+    int comp;
+    // pipelined pass: 0 waits up to the default number of polls for a tile;
+    // v > 0 waits v - 1 polls (host-side fault injection of a timeout)
+    unsigned wait_polls;
 };
 
 // a double-word constant in shared memory: hi and lo adjacent, so one
@@ -241,6 +251,14 @@ template <typename T, bool XL, int FEAT = 0> struct PassGeom {
 #ifndef GPSS_PASS_SM_THREADS_IMAGM_F32
 #define GPSS_PASS_SM_THREADS_IMAGM_F32 1024
 #endif
+// Compensated passes (FEAT_COMP) hold every transform value as hi + lo: 512
+// threads per SM (128 registers).
+#ifndef GPSS_COMP_PHASE_PLAIN
+#define GPSS_COMP_PHASE_PLAIN 0
+#endif
+#ifndef GPSS_PASS_SM_THREADS_COMP_F32
+#define GPSS_PASS_SM_THREADS_COMP_F32 512
+#endif
 #ifndef GPSS_PASS_SM_THREADS_PLANE_XL_F32
 // stacked 2D planes: 7 CTAs per SM give 64 x 256^2 planes' 2048 x tiles 1.9
 // waves instead of 2.25 (the 512-run batch 44.1 -> 43.5 ms per 500 steps)
@@ -248,7 +266,8 @@ template <typename T, bool XL, int FEAT = 0> struct PassGeom {
 #endif
 template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
     static constexpr int SM_THREADS =
-        (MODE == MODE_FUSED && (FEAT & ~FEAT_SMALL) == FEAT_NONE)
+        (FEAT & FEAT_COMP) ? GPSS_PASS_SM_THREADS_COMP_F32
+        : (MODE == MODE_FUSED && (FEAT & ~FEAT_SMALL) == FEAT_NONE)
             ? (XL ? GPSS_PASS_SM_THREADS_LEAN_XL_F32 : GPSS_PASS_SM_THREADS_LEAN_F32)
         : (MODE == MODE_FUSED && FEAT == FEAT_IMAGM)
             ? (XL ? GPSS_PASS_SM_THREADS_IMAGM_XL_F32 : GPSS_PASS_SM_THREADS_IMAGM_F32)
@@ -270,7 +289,9 @@ template <typename T, int N, bool XL, int FEAT = 0> struct PassShape {
     static constexpr int THREADS = PassGeom<T, XL, FEAT>::THREADS;
     static constexpr int W = THREADS / P;              // lines per CTA
     static constexpr int LS = N + N1 + N2;             // XL padded line stride (slots)
-    static constexpr int DATA = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
+    static constexpr int DATA1 = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
+    // compensated passes keep the lo parts in a second array of the same layout
+    static constexpr int DATA = DATA1 * ((FEAT & FEAT_COMP) ? 2 : 1);
     // w_n^{r k1} at k1*N2 + r (stage A) and at r*N1 + k1 (stage B) are the same
     // table when N1 == N2: then only one is held
     static constexpr bool TWB = N1 != N2;
@@ -299,17 +320,18 @@ __device__ __forceinline__ void block_sum_store(T v, double *partials, int q, T 
 // The last CTA of the grid to finish sums every CTA's partials (same fixed
 // order whichever CTA is last, so results are deterministic), writes the
 // sums and the next-pass factor, and re-arms the counter for the next launch.
-// CTA sums of the quantities in qmask (vals[q], q < RQ_COUNT) with one
-// barrier; thread 0 writes partials[q * gridDim.x + blockIdx.x]
-template <typename T, int THREADS>
-__device__ __forceinline__ void block_sums_store(const T (&vals)[RQ_COUNT], unsigned qmask, double *partials)
+// CTA sums of the quantities in qmask (vals[q], q < RQ_COUNT, each thread's
+// FP64 total) with one barrier, in FP64 from the thread totals on; thread 0
+// writes partials[q * gridDim.x + blockIdx.x]
+template <int THREADS>
+__device__ __forceinline__ void block_sums_store(const double (&vals)[RQ_COUNT], unsigned qmask, double *partials)
 {
-    __shared__ T red_smem[RQ_COUNT][THREADS / 32];
+    __shared__ double red_smem[RQ_COUNT][THREADS / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < RQ_COUNT; q++) {
         if (!(qmask & (1u << q))) continue;
-        T v = vals[q];
+        double v = vals[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) red_smem[q][wid] = v;
@@ -320,7 +342,7 @@ __device__ __forceinline__ void block_sums_store(const T (&vals)[RQ_COUNT], unsi
             if (!(qmask & (1u << q))) continue;
             double s = 0.0;
 #pragma unroll
-            for (int i = 0; i < THREADS / 32; i++) s += (double)red_smem[q][i];
+            for (int i = 0; i < THREADS / 32; i++) s += red_smem[q][i];
             partials[(size_t)q * gridDim.x + blockIdx.x] = s;
         }
     }
@@ -380,6 +402,8 @@ pass_kernel(const PassArgs<T> a)
     constexpr bool kAdj = kDiag || (FEAT & FEAT_ADJ) != 0;
     constexpr bool kMask = (FEAT & FEAT_MASK) != 0;
     constexpr bool kAcc = kDiag || (FEAT & FEAT_ACC) != 0;
+    constexpr bool kComp = (FEAT & FEAT_COMP) != 0 && sizeof(T) == 4;
+    static_assert(!kComp || (MODE == MODE_FUSED && !kMask && !kPlane && !kImagM), "compensated: fused kinetic passes");
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -389,6 +413,8 @@ pass_kernel(const PassArgs<T> a)
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
     V *sdata = reinterpret_cast<V *>(smem_raw);
+    V *slo = sdata + S::DATA1;  // lo parts (FEAT_COMP)
+    (void)slo;
     DWord<V> *stw = reinterpret_cast<DWord<V> *>(sdata + S::DATA);  // stage A [N], stage B [N]
     DWord<V> *stwB = S::TWB ? stw + N : stw;
     DWord<V> *sph = stw + (S::TWB ? 2 : 1) * N;                      // phase [N]
@@ -418,8 +444,11 @@ pass_kernel(const PassArgs<T> a)
     const T scale = scaled ? load_scale<T>(a.scale) : (T)1;
     const T kmult = a.kmult;
 
-    // accumulators (precision of the field; the CTA totals are kept in FP64)
+    // accumulators: the field precision within a tile (its own cells), FP64
+    // across the tiles of the CTA (one FP64 add per tile and quantity, so no
+    // FP64 arithmetic per cell), FP64 for the warp and CTA sums
     T acc_mass = 0, acc_pot = 0, acc_int = 0, acc_kin = 0, acc_rot = 0;
+    double tot[RQ_COUNT] = {0.0, 0.0, 0.0, 0.0, 0.0};
 
     // tiles of W lines; a grid smaller than the tile count loops (the tables
     // and the reduction tail are then paid once per CTA, not once per tile)
@@ -495,11 +524,110 @@ pass_kernel(const PassArgs<T> a)
                 }
             }
         }
-        dft<N1, -1>(v);
+        if constexpr (!kComp) dft<N1, -1>(v);
     }
     if constexpr (kTopBarrier) line_sync();  // the previous tile's stage B is done with sdata
 
-    if constexpr (N2 == 1) {
+    if constexpr (kComp) {
+        // compensated kinetic pass: the same stages on double-float values
+        cdf c[N1];
+        cdf_dft_from<N1, -1>(v, c);
+        if constexpr (N2 == 1) {
+            if (red & RED_KIN) {
+                T s2 = 0, s1 = 0;
+#pragma unroll
+                for (int k = 0; k < N1; k++) {
+                    const int kk = k < N / 2 ? k : k - N;
+                    const T xi = (T)kk * kmult;
+                    const T m2 = c[k].h.x * c[k].h.x + c[k].h.y * c[k].h.y;
+                    s2 += xi * xi * m2;
+                    s1 += xi * m2;
+                }
+                acc_kin += s2 * (T)(1.0 / N);
+                if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
+            }
+#pragma unroll
+            for (int k = 0; k < N1; k++) {
+                const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]} : sph[k];
+                c[k] = cdf_cmul2(c[k], p.hi, p.lo);
+                if (tscaled) c[k] = cdf_scale(c[k], tscale);
+            }
+            cdf_dft<N1, +1>(c);
+        } else {
+            // stage A store: (k1, r) <- c[k1] * w_n^{r k1}, hi and lo
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) {
+                const int m = k1 * N2 + r;
+                cdf t = c[k1];
+                if (k1 != 0 && r != 0) {
+                    const DWord<V> w2 = stw[m];
+                    t = cdf_cmul2(t, w2.hi, w2.lo);
+                }
+                sdata[sidx(m)] = t.h;
+                slo[sidx(m)] = t.l;
+            }
+            line_sync();
+            constexpr int NI = N1 / N2;
+#pragma unroll
+            for (int i = 0; i < NI; i++) {
+                const int k1 = r + P * i;
+                cdf u[N2];
+#pragma unroll
+                for (int rr = 0; rr < N2; rr++) {
+                    u[rr].h = sdata[sidx(k1 * N2 + rr)];
+                    u[rr].l = slo[sidx(k1 * N2 + rr)];
+                }
+                cdf_dft<N2, -1>(u);  // u[k2] = X[k1 + N1 k2]
+                if (red & RED_KIN) {
+                    T s2 = 0, s1 = 0;
+#pragma unroll
+                    for (int k2 = 0; k2 < N2; k2++) {
+                        const int k = k1 + N1 * k2;
+                        const int kk = k < N / 2 ? k : k - N;
+                        const T xi = (T)kk * kmult;
+                        const T m2 = u[k2].h.x * u[k2].h.x + u[k2].h.y * u[k2].h.y;
+                        s2 += xi * xi * m2;
+                        s1 += xi * m2;
+                    }
+                    acc_kin += s2 * (T)(1.0 / N);
+                    if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
+                }
+#pragma unroll
+                for (int k2 = 0; k2 < N2; k2++) {
+                    const int k = k1 + N1 * k2;
+                    const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
+                                              : sph[k];
+#if GPSS_COMP_PHASE_PLAIN
+                    u[k2].h = cmul2(u[k2].h, p.hi, p.lo);
+                    u[k2].l = cmul(u[k2].l, p.hi);
+#else
+                    u[k2] = cdf_cmul2(u[k2], p.hi, p.lo);
+#endif
+                    if (tscaled) u[k2] = cdf_scale(u[k2], tscale);
+                }
+                cdf_dft<N2, +1>(u);
+#pragma unroll
+                for (int rr = 0; rr < N2; rr++) {
+                    cdf t = u[rr];
+                    if (k1 != 0 && rr != 0) {
+                        const DWord<V> w2 = stwB[rr * N1 + k1];
+                        t = cdf_cmulc2(t, w2.hi, w2.lo);
+                    }
+                    sdata[sidx(k1 * N2 + rr)] = t.h;
+                    slo[sidx(k1 * N2 + rr)] = t.l;
+                }
+            }
+            line_sync();
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) {
+                c[k1].h = sdata[sidx(k1 * N2 + r)];
+                c[k1].l = slo[sidx(k1 * N2 + r)];
+            }
+            cdf_dft<N1, +1>(c);
+        }
+#pragma unroll
+        for (int j = 0; j < N1; j++) v[j] = c_round(c[j]);
+    } else if constexpr (N2 == 1) {
         // the whole line lives in this thread: v[k] = X[k]
         if constexpr (MODE == MODE_FUSED) {
             if (red & RED_KIN) {
@@ -783,6 +911,16 @@ pass_kernel(const PassArgs<T> a)
             for (int k = 0; k < N1; k++) a.out[base + (uint32_t)k * st] = v[k];
         }
     }
+    if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
+        if (red) {  // this tile's sums into the FP64 totals
+            tot[RQ_MASS] += (double)acc_mass;
+            tot[RQ_POT] += (double)acc_pot;
+            tot[RQ_INT] += (double)acc_int;
+            tot[RQ_KIN] += (double)acc_kin;
+            tot[RQ_ROT] += (double)acc_rot;
+            acc_mass = acc_pot = acc_int = acc_kin = acc_rot = (T)0;
+        }
+    }
 
     }  // tiles
 
@@ -801,8 +939,7 @@ pass_kernel(const PassArgs<T> a)
             if (red & (RED_POINT | RED_MASS)) qmask |= 1u << RQ_MASS;
             if (red & RED_POINT) qmask |= (1u << RQ_POT) | (1u << RQ_INT);
             if (red & RED_KIN) qmask |= (1u << RQ_KIN) | (1u << RQ_ROT);
-            const T vals[RQ_COUNT] = {acc_mass, acc_pot, acc_int, acc_kin, acc_rot};
-            block_sums_store<T, THREADS>(vals, qmask, a.partials);
+            block_sums_store<THREADS>(tot, qmask, a.partials);
             finish_reduction<T, THREADS>(a, qmask);
         }
     }

@@ -138,7 +138,7 @@ pass_pipe_kernel(const PassArgs<T> a, int ntiles)
         wait_par = (uint32_t)((it / NS) & 1);
         pref_b = nt < ntiles ? (it + 1) % NS : -1;
         pref_par = (uint32_t)(((it + 1) / NS) & 1);
-        const bool ok = mbar_wait_bounded(&bar[b], wait_par, kPipeWaitPolls);
+        const bool ok = mbar_wait_bounded(&bar[b], wait_par, a.wait_polls ? a.wait_polls - 1 : kPipeWaitPolls);
         if (__syncthreads_or(!ok)) {
             timed_out = true;
             break;

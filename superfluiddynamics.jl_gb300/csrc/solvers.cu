@@ -303,7 +303,8 @@ int gpss_rk_step(gpss_ctx *c, int nsteps, int stepper, int filter, double dt)
         return fail(c, GPSS_EINVAL, "gpss_rk_step: stepper must be 1, 2 or 4 (got %d)", stepper);
     if (filter < 0 || filter > 2) return fail(c, GPSS_EINVAL, "gpss_rk_step: filter must be 0, 1 or 2");
     if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "gpss_rk_step: dt must be finite");
-    cudaSetDevice(c->device);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     return c->precision == GPSS_FP32 ? rk_step_impl<float>(c, nsteps, stepper, filter, dt)
                                      : rk_step_impl<double>(c, nsteps, stepper, filter, dt);
 }
@@ -322,6 +323,7 @@ int gpss_implicit_step(gpss_ctx *c, int nsteps, int scheme, double dt, int nkryl
     if (!(dt > 0.0) || !std::isfinite(dt) || !(tolkrylov > 0.0) || !(tolnewton > 0.0))
         return fail(c, GPSS_EINVAL, "gpss_implicit_step: dt and the tolerances must be positive");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    GPSS_TRY(flush_pending(c));
     return c->precision == GPSS_FP32
                ? implicit_impl<float>(c, nsteps, scheme, dt, nkrylov, tolkrylov, nnewton, tolnewton, krylov_iters)
                : implicit_impl<double>(c, nsteps, scheme, dt, nkrylov, tolkrylov, nnewton, tolnewton, krylov_iters);

@@ -5,7 +5,7 @@ import numpy as np
 
 def run_model(sfd, shape, bounds, psi0, *, coeffD=-0.5, beta=1.0, omega=0.0, V=None, dt=1e-3,
               nsteps=1, scheme=2, imag=False, precision="fp64", form="fused", merge=True,
-              per_call=None, masslock=True, pipeline=False):
+              per_call=None, masslock=True, pipeline=False, compensated=False):
     g = sfd.Grid(shape, bounds)
     f = sfd.Field(g)
     f.phi = psi0
@@ -13,7 +13,7 @@ def run_model(sfd, shape, bounds, psi0, *, coeffD=-0.5, beta=1.0, omega=0.0, V=N
     p = sfd.GrossPitaevskiiParameters(pot, coeffD=coeffD, beta=beta, Omega=omega)
     cls = sfd.NumModelSplit2 if scheme == 2 else sfd.NumModelSplit1
     n = cls(f, p, dt, nsteps, nsteps, precision=precision, form=form, merge=merge, masslock=masslock,
-            pipeline=pipeline)
+            pipeline=pipeline, compensated=compensated)
     done = 0
     k = per_call or nsteps
     while done < nsteps:

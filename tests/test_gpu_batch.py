@@ -81,3 +81,33 @@ def test_batch_golden_cfg3_runs(sfd, O):
         cell = np.prod([(r[1] - r[0]) / m for r, m in zip(z["bounds"], z["psi0"].shape)])
         assert abs(masses[i] * cell - z["trace_mass"][-1]) <= 1e-6 * z["trace_mass"][-1]
     b.close()
+
+
+def test_batch_full_cfg3_vs_oracle(sfd, O, W):
+    """The full cfg3 batch the bench times: 512 runs (256 x 64^2, 192 x 128^2,
+    64 x 256^2), 500 steps in one call, autotuned launch.  Every 256^2 run and
+    16 runs of each smaller size against the FP64 oracle within 1e-5; every
+    run's FP64 mass sum within 1e-6 of its initial mass."""
+    c = W.cfg3()
+    runs = c["runs"]
+    b = sfd.BatchSplit2([r["n"] for r in runs], [r["bounds"] for r in runs], coeffD=c["coeffD"])
+    for i, r in enumerate(runs):
+        b.set_run(i, r["beta"], r["V"], r["psi"])
+    masses = b.step(c["nsteps"], c["dt"])
+    picked = [i for i, r in enumerate(runs) if r["n"] == 256]
+    for n in (64, 128):
+        idx = [i for i, r in enumerate(runs) if r["n"] == n]
+        picked += idx[:: len(idx) // 16][:16]
+    worst = 0.0
+    for i in picked:
+        r = runs[i]
+        ref = O.c_step(r["psi"], r["bounds"], coeffD=c["coeffD"], beta=r["beta"], V=r["V"], nsteps=c["nsteps"],
+                       dt=c["dt"])
+        err = O.rel_l2(b.download(i), ref)
+        worst = max(worst, err)
+        assert err < 1e-5, (i, r["n"], r["beta"], err)
+    for i, r in enumerate(runs):
+        m0 = np.sum(np.abs(r["psi"].astype(np.complex64)) ** 2)
+        assert abs(masses[i] - m0) / m0 < 1e-6
+    print(f"cfg3 full batch: {len(picked)} runs vs the oracle, worst rel-L2 {worst:.2e}")
+    b.close()

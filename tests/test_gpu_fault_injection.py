@@ -7,6 +7,7 @@ import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -67,3 +68,33 @@ def test_allocation_failures_are_reported():
             seen_rk_fail = True
             break
     assert seen_create_fail and seen_rk_fail
+
+
+def test_pipelined_wait_timeout_is_reported(sfd, O):
+    """The pipelined x pass bounds every wait on a tile's barrier.  With
+    GPSS_FAULT_PIPE_POLLS=0 every CTA gives up at once (no GPU fault: each CTA
+    still waits, bounded, for the copies it issued before it returns): the step
+    returns GPSS_ETIMEOUT, and the same context then steps normally, bitwise
+    equal to the direct kernel."""
+    from helpers import random_field, run_model
+    shape, bounds = (64, 32, 16), ((-4.0, 4.0), (-3.0, 3.0), (-2.0, 2.0))
+    psi0 = random_field(shape, seed=17)
+    kw = dict(coeffD=-0.5, beta=2.0, dt=1e-3, nsteps=4, precision="fp32", masslock=False)
+    g = sfd.Grid(shape, bounds)
+    f = sfd.Field(g)
+    f.phi = psi0
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=-0.5, beta=2.0)
+    n = sfd.NumModelSplit2(f, p, 1e-3, 4, 4, precision="fp32", pipeline=True, masslock=False)
+    os.environ["GPSS_FAULT_PIPE_POLLS"] = "0"
+    try:
+        with pytest.raises(sfd.GPSSError) as ei:
+            n.step(4)
+    finally:
+        del os.environ["GPSS_FAULT_PIPE_POLLS"]
+    assert "ETIMEOUT" in str(ei.value) or "gave up" in str(ei.value)
+    f.phi = psi0  # the context is still usable
+    n.step(4)
+    got = f.phi.copy()
+    n.close()
+    ref = run_model(sfd, shape, bounds, psi0, pipeline=False, **kw)
+    assert np.array_equal(got, ref)

@@ -127,6 +127,21 @@ def test_c_oracle_matches_numpy_oracle(O, imag, scheme, shape):
     assert O.rel_l2(O.c_step(p, b, **kw), O.np_step(p, b, **kw)) < 1e-13
 
 
+def test_timed_legs_match_the_oracle(O):
+    """The timing legs of the CPU baseline step the same field as c_step: the
+    loop-timed C entry point bit for bit, the scipy.fft restatement to FP64
+    round-off; both report a positive loop time."""
+    shape, bounds = (16, 8, 32), ((0.0, 6.0), (0.0, 5.0), (0.0, 7.0))
+    rng = np.random.default_rng(3)
+    psi = np.asfortranarray(np.exp(1j * rng.uniform(0, 0.3, shape)))
+    kw = dict(coeffD=-0.0353, beta=14.1, nsteps=4, dt=2.5e-3)
+    ref = O.c_step(psi, bounds, **kw)
+    a, ta = O.c_step_timed(psi, bounds, **kw)
+    b, tb = O.sp_step_timed(psi, bounds, workers=2, **kw)
+    assert np.array_equal(a, ref) and ta > 0
+    assert O.rel_l2(b, ref) < 1e-13 and tb > 0
+
+
 def test_energy_formulas(O):
     """Derivative route of GrossPitaevskii.jl:61-136 vs a Parseval evaluation."""
     shape, b = (32, 16, 8), ((-5.0, 6.0),) * 3
