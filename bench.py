@@ -723,6 +723,28 @@ def run_gpss(args, rank, world, local):
                  "unit": "Mcell-steps/s", "ms_per_step": t2 / k2, "steps": k2,
                  "roofline": roofline(per2, "fp32" if comp else "fp32c", t2 / k2)}
 
+    # ---- measured FMA roofs (FP32 for the compensated passes, FP64 for the
+    # FP64 kernels): both are bound by their FMA pipe, not by HBM
+    peaks = {}
+    for prec, key in ((32, "fp32_tflops"), (64, "fp64_tflops")):
+        t = ctypes.c_double()
+        if L.gpss_measure_fma_rate(prec, ctypes.byref(t)) == 0:
+            peaks[key] = t.value
+    # algorithmic flops per cell and time step (5 n log2 n per length-n FFT,
+    # 6 per complex phase multiply, ~20 for the nonlinear factor): merged
+    # step = 3 kinetic flows; the plain form = 2 half-step flows of 3 axes
+    lg = math.log2(args.n)
+    flops_merged = 3 * (2 * 5 * lg + 6) + 20
+    flops_plain = 2 * 3 * (2 * 5 * lg + 6) + 20
+    if peaks.get("fp32_tflops"):
+        ach = flops_merged * value / world * 1e6 / 1e12
+        roof["compute"] = {"unit": "TFLOP/s", "algorithmic_flops_per_cell_step": flops_merged,
+                           "achieved": ach, "fp32_fma_peak_measured": peaks["fp32_tflops"],
+                           "frac": ach / peaks["fp32_tflops"],
+                           "note": "algorithmic flops of the merged step; the compensated arithmetic executes "
+                                   "several times more FP32 operations than that count (the FMA-pipe "
+                                   "utilisation from ncu is in profiles/)"}
+
     # ---- FP64 plain kernels on the same workload (fewer time steps)
     fp64 = None
     if not args.no_fp64:
@@ -742,6 +764,11 @@ def run_gpss(args, rank, world, local):
         v64 = cells * k64 / (ms64.value / 1e3) / 1e6
         fp64 = {"value": v64, "unit": "Mcell-steps/s", "timesteps": k64,
                 "ms_per_timestep": ms64.value / k64, "fp32_over_fp64_plain": value / world / v64}
+        if peaks.get("fp64_tflops"):
+            ach64 = flops_plain * v64 * 1e6 / 1e12
+            fp64["roofline"] = {"bound": "fp64_fma", "unit": "TFLOP/s", "algorithmic_flops_per_cell_step": flops_plain,
+                                "achieved": ach64, "peak": peaks["fp64_tflops"], "frac": ach64 / peaks["fp64_tflops"],
+                                "peak_source": "gpss_measure_fma_rate (FP64 FMA chains, CUDA events)"}
         if other:
             other["fp32_over_fp64_plain"] = other["value"] / v64
 
@@ -797,6 +824,7 @@ def run_gpss(args, rank, world, local):
         "e2e": None if e2e is None else {"value": e2e, "unit": "Mcell-steps/s", "h2d_bytes_per_step": nbytes,
                                          "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
         "roofline": roof,
+        "fma_peaks_measured": peaks,
         "cpu_baseline": cpu,
         "fp64_plain": fp64,
         ("fp32_plain" if comp else "fp32_compensated"): other,

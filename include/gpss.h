@@ -84,7 +84,13 @@ const char *gpss_version(void);
  * [x n[2]] nodes on [lo[a], hi[a]).  Replaces Grid(size, bounds)
  * (src/Discretization/Grids.jl:64-129) + Field(grid, ComplexField())
  * (src/Discretization/Fields.jl:94-157) + Plan(f) (src/Discretization/Plans.jl:821-854,
- * 958-999).  ndim is 2 or 3; each n[a] is a power of two in [2, 256].
+ * 958-999).  ndim is 2 or 3; each n[a] is in [2, 1024] with no prime factor
+ * above 31 (the reference plans any length with FFTW, Plans.jl:846-847).
+ * Powers of two up to 256 run the register-resident pass kernels; other
+ * lengths run the mixed-radix shared-memory pass, which takes every split,
+ * energy, explicit RK and implicit entry point but not GPSS_FLAG_COMPENSATED
+ * or gpss_adjoint (those return GPSS_EINVAL); the merged imaginary-time step
+ * then runs as the unmerged sequence.
  * precision is GPSS_FP64 or GPSS_FP32; flags is a GPSS_FLAG_* mask.
  */
 int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, const double *hi,
@@ -300,6 +306,15 @@ int64_t gpss_launch_count(const gpss_ctx *ctx);
  * milliseconds per launch.  The field is advanced by those launches.
  */
 int gpss_time_pass(gpss_ctx *ctx, int axis, int mode, int reps, double dt, double *ms_per_launch);
+
+/*
+ * FMA throughput of the current device in TFLOP/s (2 flops per fused
+ * multiply-add; precision GPSS_FP32 or GPSS_FP64), measured with CUDA events
+ * on a kernel of independent FMA chains.  A diagnostic: it is the compute roof
+ * for the roofline reports of the FP64 kernels and of the compensated FP32
+ * passes, which their FMA pipe bounds.  No counterpart in the reference.
+ */
+int gpss_measure_fma_rate(int precision, double *tflops);
 
 /* Page-locked host buffer helpers for fast uploads/downloads. */
 int gpss_host_alloc(void **ptr, int64_t bytes);

@@ -105,6 +105,7 @@ SIGNATURES = {
     "gpss_select_device": (ctypes.c_int, [ctypes.c_int]),
     "gpss_device_count": (ctypes.c_int, []),
     "gpss_host_alloc": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int64]),
+    "gpss_measure_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "gpss_host_free": (ctypes.c_int, [_vp]),
     "gpss_device_bytes": (ctypes.c_int64, [_vp]),
     "gpss_energy_noalloc": (ctypes.c_int, [ctypes.c_int, _i64p, _f64p, _f64p, ctypes.c_int, ctypes.c_double,

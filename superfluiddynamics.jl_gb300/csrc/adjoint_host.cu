@@ -291,6 +291,8 @@ int gpss_adjoint(gpss_ctx *c, const double *psi_target, int nsteps, int K, doubl
     if (nsteps < 1 || K < 1) return fail(c, GPSS_EINVAL, "gpss_adjoint: need nsteps >= 1 and K >= 1");
     if (!std::isfinite(dt)) return fail(c, GPSS_EINVAL, "dt must be finite");
     if (!c->have_psi) return fail(c, GPSS_ESTATE, "no field uploaded");
+    if (any_generic(c))
+        return fail(c, GPSS_EINVAL, "gpss_adjoint: every axis must be a power of two of at most 256");
     CUDA_TRY(c, cudaSetDevice(c->device));
     GPSS_TRY(flush_pending(c));
     if (c->precision == GPSS_FP32) return adjoint_impl<float>(c, psi_target, nsteps, K, dt, loss, dLdV, dLdpsi0);

@@ -58,7 +58,10 @@ struct gpss_ctx {
     void *psi = nullptr;      // device field (float2 or double2)
     void *scratch = nullptr;  // spectrum (plain form) and FP64 staging, total*16 bytes
     void *V = nullptr;        // device potential (float or double)
-    void *tw[3] = {nullptr, nullptr, nullptr};
+    void *tw[3] = {nullptr, nullptr, nullptr};  // per axis: register-kernel twiddles, or the generic pass's roots
+    // axes whose lines the generic pass runs (not a power of two in [2, 256])
+    bool gen[3] = {false, false, false};
+    GenPlan gplan[3] = {};
     double *coord_dev[3] = {nullptr, nullptr, nullptr};
     std::vector<double> coord[3];
     double *partials = nullptr;
@@ -318,8 +321,11 @@ template <typename T> static PassArgs<T> axis_args(gpss_ctx *c, int axis, const 
     return a;
 }
 
+static bool any_generic(const gpss_ctx *c) { return c->gen[0] || c->gen[1] || c->gen[2]; }
+
 template <typename T> static int blocks_for(gpss_ctx *c, int axis)
 {
+    if (c->gen[axis]) return (int)((c->total / c->n[axis] + c->gplan[axis].W - 1) / c->gplan[axis].W);
     const int W = PassLauncher<T>::lines((int)c->n[axis], axis == 0);
     const int64_t nl = c->total / c->n[axis];
     return (int)((nl + W - 1) / W);
@@ -366,6 +372,14 @@ template <typename T> static int launch(gpss_ctx *c, int axis, int mode, const P
         cudaError_t e = PassLauncher<T>::pipe(axis == 0, (int)c->n[axis], ap, ntiles, c->stream);
         if (e != cudaSuccess)
             return fail(c, GPSS_ECUDA, "pipelined pass launch (axis %d): %s", axis, cudaGetErrorString(e));
+        c->launches++;
+        return GPSS_OK;
+    }
+    if (c->gen[axis]) {
+        cudaError_t e = PassLauncher<T>::gen(mode, a, c->gplan[axis], c->stream);
+        if (e != cudaSuccess)
+            return fail(c, GPSS_ECUDA, "generic pass launch (axis %d, n = %lld, mode %d): %s", axis,
+                        (long long)c->n[axis], mode, cudaGetErrorString(e));
         c->launches++;
         return GPSS_OK;
     }

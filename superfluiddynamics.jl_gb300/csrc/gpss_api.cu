@@ -255,7 +255,8 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
             c->pending_h = dt * 0.5;
             c->pending_scale = lock;
         }
-    } else if (imag && scheme == GPSS_STRANG && c->omega == 0.0 && !(c->flags & GPSS_FLAG_NOMERGE)) {
+    } else if (imag && scheme == GPSS_STRANG && c->omega == 0.0 && !(c->flags & GPSS_FLAG_NOMERGE) &&
+               !any_generic(c)) {
         GPSS_TRY(imag_merged<T>(c, nsteps, dt));
     } else if (imag) {
         for (int s = 0; s < nsteps; s++) {
@@ -321,7 +322,6 @@ static int step_impl(gpss_ctx *c, int nsteps, int scheme, int imag, double dt, g
 }
 
 
-static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
 extern "C" {
 
@@ -370,19 +370,32 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if (flags & ~(GPSS_FLAG_PLAIN | GPSS_FLAG_NOMERGE | GPSS_FLAG_NOMASSLOCK | GPSS_FLAG_PIPE | GPSS_FLAG_ENERGY_CACHE |
                   GPSS_FLAG_COMPENSATED))
         return fail(nullptr, GPSS_EINVAL, "unknown flags 0x%x", flags);
+    bool any_gen = false;
     for (int a = 0; a < ndim; a++) {
-        if (!is_pow2(n[a]) || n[a] < 2 || n[a] > 256)
-            return fail(nullptr, GPSS_EINVAL, "n[%d] = %lld: each axis must be a power of two in [2, 256]", a,
-                        (long long)n[a]);
+        GenPlan gp;
+        if (!reg_line(n[a]) && !(n[a] >= 2 && n[a] <= GEN_MAX_N && gen_plan_radices((int)n[a], gp)))
+            return fail(nullptr, GPSS_EINVAL,
+                        "n[%d] = %lld: each axis needs 2 <= n <= %d cells with no prime factor above 31", a,
+                        (long long)n[a], GEN_MAX_N);
+        any_gen = any_gen || !reg_line(n[a]);
         if (!(hi[a] > lo[a]) || !std::isfinite(lo[a]) || !std::isfinite(hi[a]))
             return fail(nullptr, GPSS_EINVAL, "axis %d: need finite lo < hi", a);
     }
+    if (any_gen && (flags & GPSS_FLAG_COMPENSATED))
+        return fail(nullptr, GPSS_EINVAL, "GPSS_FLAG_COMPENSATED needs every axis to be a power of two of at most 256");
     gpss_ctx *c = new (std::nothrow) gpss_ctx();
     if (!c) return fail(nullptr, GPSS_ENOMEM, "host allocation failed");
     c->ndim = ndim;
     c->precision = precision;
     c->flags = flags;
     c->total = 1;
+    for (int a = 0; a < ndim; a++) {
+        c->gen[a] = !reg_line(n[a]);
+        if (c->gen[a]) {
+            gen_plan_radices((int)n[a], c->gplan[a]);
+            c->gplan[a].W = gen_tile_lines((int)n[a], precision == GPSS_FP32 ? 4 : 8);
+        }
+    }
     for (int a = 0; a < 3; a++) {
         c->n[a] = a < ndim ? n[a] : 1;
         c->lo[a] = a < ndim ? lo[a] : 0.0;
@@ -411,10 +424,23 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     // twiddles per axis, stage-A layout m = k1*N2 + r: exp(-2 pi i r k1 / n) as hi + lo
     for (int a = 0; a < ndim; a++) {
         const int64_t na = c->n[a];
-        // two rows: stage-A order (k1*N2 + r) and stage-B order (r*N1 + k1)
         std::vector<ldouble> re, im;
-        twiddle_rows(na, re, im);
-        if ((rc = upload_dw(c, &c->tw[a], re, im, 2, na))) return bail(rc);
+        if (c->gen[a]) {
+            // generic pass: the roots w_n^k = exp(-2 pi i k / n), k < n
+            re.resize((size_t)na);
+            im.resize((size_t)na);
+            for (int64_t k = 0; k < na; k++) {
+                ldouble cs, sn;
+                unit_root(k, na, &cs, &sn);
+                re[(size_t)k] = cs;
+                im[(size_t)k] = -sn;
+            }
+            if ((rc = upload_dw(c, &c->tw[a], re, im, 1, na))) return bail(rc);
+        } else {
+            // two rows: stage-A order (k1*N2 + r) and stage-B order (r*N1 + k1)
+            twiddle_rows(na, re, im);
+            if ((rc = upload_dw(c, &c->tw[a], re, im, 2, na))) return bail(rc);
+        }
         if ((rc = dev_alloc(c, (void **)&c->coord_dev[a], sizeof(double) * (size_t)c->n[a]))) return bail(rc);
         e = cudaMemcpy(c->coord_dev[a], c->coord[a].data(), sizeof(double) * (size_t)c->n[a], cudaMemcpyHostToDevice);
         if (e != cudaSuccess) { fail(c, GPSS_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e)); return bail(GPSS_ECUDA); }

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 #include "pass_kernel.cuh"
+#include "pass_generic.cuh"
 
 namespace gpss {
 
@@ -87,6 +88,10 @@ int pass_lines_per_cta_f64(int n, bool xl);
 cudaError_t launch_pipe_f32(bool xl, int n, const PassArgs<float> &a, int ntiles, cudaStream_t s);
 cudaError_t launch_pipe_f64(bool xl, int n, const PassArgs<double> &a, int ntiles, cudaStream_t s);
 
+// the generic-length pass (pass_gen.cu)
+cudaError_t launch_gen_f32(int mode, const PassArgs<float> &a, const GenPlan &p, cudaStream_t s);
+cudaError_t launch_gen_f64(int mode, const PassArgs<double> &a, const GenPlan &p, cudaStream_t s);
+
 template <typename T> struct PassLauncher;
 template <> struct PassLauncher<float> {
     static cudaError_t launch(int mode, bool xl, int n, const PassArgs<float> &a, int blocks,
@@ -95,6 +100,10 @@ template <> struct PassLauncher<float> {
     static cudaError_t pipe(bool xl, int n, const PassArgs<float> &a, int ntiles, cudaStream_t s)
     {
         return launch_pipe_f32(xl, n, a, ntiles, s);
+    }
+    static cudaError_t gen(int mode, const PassArgs<float> &a, const GenPlan &p, cudaStream_t s)
+    {
+        return launch_gen_f32(mode, a, p, s);
     }
 };
 template <> struct PassLauncher<double> {
@@ -105,7 +114,27 @@ template <> struct PassLauncher<double> {
     {
         return launch_pipe_f64(xl, n, a, ntiles, s);
     }
+    static cudaError_t gen(int mode, const PassArgs<double> &a, const GenPlan &p, cudaStream_t s)
+    {
+        return launch_gen_f64(mode, a, p, s);
+    }
 };
+
+// Lines per tile of the generic pass: as many as fit about 96 KB of shared
+// memory (two buffers), at most 16 (FP32) / 8 (FP64) -- 128-byte rows of
+// adjacent columns for the y/z passes.
+inline int gen_tile_lines(int n, int precision_bytes)
+{
+    const size_t per_line = 2 * (size_t)n * 2 * (size_t)precision_bytes;
+    int W = (int)((96u * 1024u) / per_line);
+    const int cap = precision_bytes == 4 ? 16 : 8;
+    if (W > cap) W = cap;
+    return W < 1 ? 1 : W;
+}
+
+// Is a line of n cells taken by the register kernel (a power of two up to
+// 256)?  Otherwise the generic pass runs it.
+inline bool reg_line(int64_t n) { return n >= 2 && n <= 256 && (n & (n - 1)) == 0; }
 
 // pointwise kernels (pointwise.cu)
 cudaError_t launch_f64_to_f32(const double *in, float *out, int64_t count, cudaStream_t s);

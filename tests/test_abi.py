@@ -42,8 +42,10 @@ def _create(L, ndim, n, lo, hi, prec=64, flags=0):
 
 @pytest.mark.parametrize("ndim,n,lo,hi,prec,flags", [
     (1, (32,), (0,), (1,), 64, 0),              # 1D is not a split-step field here
-    (2, (48, 32), (0, 0), (1, 1), 64, 0),       # not a power of two
-    (2, (512, 32), (0, 0), (1, 1), 64, 0),      # above 256 per axis
+    (2, (37, 32), (0, 0), (1, 1), 64, 0),       # prime factor above 31
+    (2, (32, 74), (0, 0), (1, 1), 64, 0),       # 2 x 37
+    (2, (2048, 32), (0, 0), (1, 1), 64, 0),     # above 1024 per axis
+    (2, (48, 32), (0, 0), (1, 1), 32, 32),      # compensated passes need powers of two up to 256
     (2, (1, 32), (0, 0), (1, 1), 64, 0),        # below 2
     (2, (32, 32), (1, 0), (1, 1), 64, 0),       # lo == hi
     (2, (32, 32), (0, 0), (1, 1), 16, 0),       # unknown precision

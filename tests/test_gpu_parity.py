@@ -677,3 +677,28 @@ def test_energy_cache_rotation_vs_oracle(sfd, O, shape):
         scale = max(abs(v) for v in e_ref[:4])
         assert np.max(np.abs(row[2:6] - np.array(e_ref[:4]))) <= 1e-11 * scale
         ref = O.c_step(ref, bounds, nsteps=1, dt=2e-3, **kw)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-14), ("fp32", 2e-7)])
+def test_device_norm_and_normalize(sfd, O, precision, tol):
+    """norm(f) and normalize!(f) (Fields.jl:172-200) on a model-owned field run
+    on the device (gpss_norm, gpss_normalize: FP64 sums) and match the oracle's
+    c_norm; after a step (whose last half flow may be pending) too."""
+    shape, bounds = (64, 32, 16), ((-4.0, 4.0), (-3.0, 5.0), (-2.0, 2.0))
+    psi0 = 3.7 * random_field(shape, seed=51)
+    g = sfd.Grid(shape, bounds)
+    f = sfd.Field(g)
+    f.phi = psi0
+    p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=-0.5, beta=2.0)
+    n = sfd.NumModelSplit2(f, p, 1e-3, 1, 1, precision=precision)
+    src = psi0.astype(np.complex64).astype(np.complex128) if precision == "fp32" else psi0
+    want = O.c_norm(src, bounds)
+    assert abs(sfd.norm(f) - want) <= tol * want
+    sfd.normalize(f)
+    assert abs(sfd.norm(f) - 1.0) <= tol
+    assert O.rel_l2(f.phi, src / want) <= tol
+    n.step(3)  # leaves its last half kinetic flow pending: norm applies it first
+    nrm = sfd.norm(f)
+    after = f.phi.copy()
+    assert abs(nrm - O.c_norm(after, bounds)) <= 2 * tol
+    n.close()
