@@ -1,25 +1,39 @@
 // fft_comp.cuh -- compensated FP32 arithmetic for the directional passes:
-// small DFTs (sizes 1, 2, 4, 8, 16) on double-float complex values.
+// small DFTs (sizes 2, 4, 8, 16) on two-float complex values whose high part
+// lives on a power-of-two grid.
 //
-// A value is hi + lo, both float2 (re, im).  Every addition keeps its exact
-// rounding error (Knuth's TwoSum, six operations) and every product by a
-// double-word constant its exact error (the FMA residual a*b - RN(a*b));
-// those errors, and the lo parts of the inputs, travel through the rest of
-// the transform as a second, linear FP32 computation.  The lo parts are about
-// 2^-24 of the hi parts, so their own rounding is about 2^-48 of the value:
-// the transform is accurate to near-FP64 level on FP32 instructions, and the
-// only FP32 rounding left in a pass is the store of the field.
+// A value is h + l (both float2: re, im).  Within one transform stage a
+// thread picks a quantum q (a power of two, 2^-17 of a bound of the stage's
+// input magnitudes) and keeps every h an integer multiple of q with
+// |h| < 2^22 q.  Then:
+//   * the sum of two h is exact (a multiple of q below 2^24 q), so a complex
+//     add is two FP32 adds, h + h and l + l;
+//   * a product h * c by a double-word constant c_hi + c_lo is split into
+//     its rounding to the grid, fma(h, c_hi, C) - C with C = 1.5 * 2^23 q
+//     (one rounding of the exact product), and the exact residual
+//     fma(h, c_hi, -that), which goes to l together with h * c_lo + l * c_hi;
+//   * l only collects residuals of size ~q, so its own FP32 rounding is
+//     ~2^-24 q: about 2^-41 of the stage's largest input, far below FP32.
+// A stage's values grow at most 16 sqrt(2) (< 32) times its input bound
+// (one DFT-16 and unit-modulus twiddles; the kinetic phase factors include
+// 1/n), which is the headroom 2^22 q = 2^5 * 2^E above a bound 2^E of the
+// input.  Between stages (through shared memory) each thread re-grids the
+// values it gathers on its own quantum: h' = RN_q'(h), l' = l + (h - h'),
+// exact except for the l add.
+//
+// Cost per complex operation in packed f32x2 instructions: add 2, product by
+// a double-word constant 12, entering the grid 3; against 8 / 16 for
+// double-float arithmetic with TwoSum additions.
 //
 // This matters where the time stepping amplifies round-off: at the 256^3
 // quantum-turbulence workload (coeffD = -0.0354, dt = 2.5e-3) the modes with
 // |coeffD| |k|^2 dt near pi grow by about 2.7x per 25 steps (the split-step
-// resonance), and the rounding noise of plain FP32 FFTs is the seed that they
-// grow from.
+// resonance), and the rounding noise of plain FP32 FFTs is the seed that
+// they grow from.
 //
-// All operations are packed f32x2 instructions (add/sub/mul/fma.rn.f32x2),
-// one instruction per complex component pair, written as inline PTX so the
-// compiler can neither contract nor reassociate them (the error terms rely on
-// the exact IEEE round-to-nearest results).
+// All operations are packed f32x2 instructions (add/sub/mul/fma.rn.f32x2)
+// written as inline PTX, so the compiler can neither contract nor
+// reassociate them ((x + C) - C must round x to the grid).
 #pragma once
 #include <cuda_runtime.h>
 #include "fft_core.cuh"
@@ -69,129 +83,121 @@ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c)
 }
 __device__ __forceinline__ float2 p_neg(float2 a) { return make_float2(-a.x, -a.y); }
 
-// s + e == a + b exactly (per component)
-__device__ __forceinline__ void two_sum(float2 a, float2 b, float2 &s, float2 &e)
+// ---------------------------------------------------------------- the grid --
+// C = 1.5 * 2^23 * q (both lanes) for the quantum q = 2^(E - 17), E the
+// exponent with m < 2^E.  q is kept a normal number (m below 2^-109 uses the
+// smallest such grid; those values then ride in l at FP32 precision) and C
+// finite.
+__device__ __forceinline__ float2 grid_for(float m)
 {
-    s = p_add(a, b);
-    const float2 bb = p_sub(s, a);
-    e = p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb));
-}
-// s + e == a - b exactly
-__device__ __forceinline__ void two_diff(float2 a, float2 b, float2 &s, float2 &e)
-{
-    s = p_sub(a, b);
-    const float2 bb = p_sub(s, a);  // ~ -b
-    e = p_sub(p_sub(a, p_sub(s, bb)), p_add(b, bb));
+    int e = (int)((__float_as_uint(m) >> 23) & 0xffu);  // m in [2^(e-127), 2^(e-126))
+    e = e < 17 ? 17 : (e > 247 ? 247 : e);
+    const float C = __uint_as_float(((unsigned)(e + 7) << 23) | 0x400000u);
+    return make_float2(C, C);
 }
 
-__device__ __forceinline__ cdf c_of(float2 h) { return cdf{h, make_float2(0.f, 0.f)}; }
-// hi + lo rounded once to FP32
+// bound of |re|, |im| over NV values (ALU min/max; the inputs of one stage)
+template <int NV> __device__ __forceinline__ float absmax(const float2 *x)
+{
+    float m = 0.f;
+#pragma unroll
+    for (int i = 0; i < NV; i++) m = fmaxf(m, fmaxf(fabsf(x[i].x), fabsf(x[i].y)));
+    return m;
+}
+template <int NV> __device__ __forceinline__ float absmax(const cdf *x)
+{
+    float mh = 0.f, ml = 0.f;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        mh = fmaxf(mh, fmaxf(fabsf(x[i].h.x), fabsf(x[i].h.y)));
+        ml = fmaxf(ml, fmaxf(fabsf(x[i].l.x), fabsf(x[i].l.y)));
+    }
+    return mh + ml;
+}
+
+// FP32 x onto the grid: h = RN_q(x), l = x - h (exact)
+__device__ __forceinline__ cdf g_from(float2 x, float2 C)
+{
+    const float2 h = p_sub(p_add(x, C), C);
+    return cdf{h, p_sub(x, h)};
+}
+// FP32 x times an FP32 scale s onto the grid: h = RN_q(x s), l = x s - h
+// (the exact residual, one FP32 rounding of a value below q)
+__device__ __forceinline__ cdf g_from_scaled(float2 x, float2 s, float2 C)
+{
+    const float2 h = p_sub(p_fma(x, s, C), C);
+    return cdf{h, p_fma(x, s, p_neg(h))};
+}
+// a value from another thread's grid onto this one
+__device__ __forceinline__ cdf g_regrid(const cdf &a, float2 C)
+{
+    const float2 h = p_sub(p_add(a.h, C), C);
+    return cdf{h, p_add(a.l, p_sub(a.h, h))};
+}
+// h + l rounded once to FP32
 __device__ __forceinline__ float2 c_round(const cdf &a) { return p_add(a.h, a.l); }
 
-__device__ __forceinline__ cdf cdf_add(const cdf &a, const cdf &b)
-{
-    cdf r;
-    float2 e;
-    two_sum(a.h, b.h, r.h, e);
-    r.l = p_add(p_add(a.l, b.l), e);
-    return r;
-}
-__device__ __forceinline__ cdf cdf_sub(const cdf &a, const cdf &b)
-{
-    cdf r;
-    float2 e;
-    two_diff(a.h, b.h, r.h, e);
-    r.l = p_add(p_sub(a.l, b.l), e);
-    return r;
-}
-// exact sum / difference of two FP32 values (the first butterfly level of a
-// transform whose inputs are the stored field)
-__device__ __forceinline__ cdf cdf_add0(float2 a, float2 b)
-{
-    cdf r;
-    two_sum(a, b, r.h, r.l);
-    return r;
-}
-__device__ __forceinline__ cdf cdf_sub0(float2 a, float2 b)
-{
-    cdf r;
-    two_diff(a, b, r.h, r.l);
-    return r;
-}
+__device__ __forceinline__ cdf g_add(const cdf &a, const cdf &b) { return cdf{p_add(a.h, b.h), p_add(a.l, b.l)}; }
+__device__ __forceinline__ cdf g_sub(const cdf &a, const cdf &b) { return cdf{p_sub(a.h, b.h), p_sub(a.l, b.l)}; }
 
 // multiply by DIR*i (exact)
-template <int DIR> __device__ __forceinline__ cdf cdf_muli(const cdf &a)
+template <int DIR> __device__ __forceinline__ cdf g_muli(const cdf &a)
 {
     if (DIR < 0) return cdf{make_float2(a.h.y, -a.h.x), make_float2(a.l.y, -a.l.x)};
     return cdf{make_float2(-a.h.y, a.h.x), make_float2(-a.l.y, a.l.x)};
 }
-__device__ __forceinline__ cdf cdf_neg(const cdf &a) { return cdf{p_neg(a.h), p_neg(a.l)}; }
+__device__ __forceinline__ cdf g_neg(const cdf &a) { return cdf{p_neg(a.h), p_neg(a.l)}; }
 
-// a * s for a real FP32 scalar s (exact product error kept)
-__device__ __forceinline__ cdf cdf_scale(const cdf &a, float s)
-{
-    const float2 ss = make_float2(s, s);
-    cdf r;
-    r.h = p_mul(a.h, ss);
-    const float2 e = p_fma(a.h, ss, p_neg(r.h));
-    r.l = p_fma(a.l, ss, e);
-    return r;
-}
 // a * (hi + lo) for a real double-word constant
-__device__ __forceinline__ cdf cdf_rmul2(const cdf &a, float hi, float lo)
+__device__ __forceinline__ cdf g_rmul2(const cdf &a, float hi, float lo, float2 C)
 {
     const float2 H = make_float2(hi, hi), L = make_float2(lo, lo);
-    cdf r;
-    r.h = p_mul(a.h, H);
-    const float2 e = p_fma(a.h, H, p_neg(r.h));
-    r.l = p_fma(a.h, L, p_fma(a.l, H, e));
-    return r;
+    const float2 h = p_sub(p_fma(a.h, H, C), C);
+    const float2 r = p_fma(a.h, H, p_neg(h));
+    return cdf{h, p_fma(a.h, L, p_fma(a.l, H, r))};
 }
 
-// a * (bh + bl), b a double-word complex constant:
-//   re = ax bx - ay by, im = ax by + ay bx as packed pairs
-//   (ax, ax)*(bx, by) + (ay, ay)*(-by, bx)
-__device__ __forceinline__ cdf cdf_cmul2(const cdf &a, float2 bh, float2 bl)
+// a * (bh + bl), b a double-word complex constant, as packed pairs:
+//   (re, im) = (ax, ax) * (bx, by) + (ay, ay) * (-by, bx)
+// each of the two packed products is gridded with its exact residual
+__device__ __forceinline__ cdf g_cmul2(const cdf &a, float2 bh, float2 bl, float2 C)
 {
     const float2 X = make_float2(a.h.x, a.h.x), Y = make_float2(a.h.y, a.h.y);
     const float2 b2 = make_float2(-bh.y, bh.x), bl2 = make_float2(-bl.y, bl.x);
-    const float2 p1 = p_mul(X, bh), p2 = p_mul(Y, b2);
-    const float2 e1 = p_fma(X, bh, p_neg(p1)), e2 = p_fma(Y, b2, p_neg(p2));
-    cdf r;
-    float2 es;
-    two_sum(p1, p2, r.h, es);
-    float2 l = p_add(p_add(e1, e2), es);
+    const float2 u = p_sub(p_fma(X, bh, C), C);
+    const float2 v = p_sub(p_fma(Y, b2, C), C);
+    float2 l = p_add(p_fma(X, bh, p_neg(u)), p_fma(Y, b2, p_neg(v)));
     l = p_fma(X, bl, l);
     l = p_fma(Y, bl2, l);
     l = p_fma(make_float2(a.l.x, a.l.x), bh, l);
     l = p_fma(make_float2(a.l.y, a.l.y), b2, l);
-    r.l = l;
-    return r;
+    return cdf{p_add(u, v), l};
 }
 // a * conj(bh + bl)
-__device__ __forceinline__ cdf cdf_cmulc2(const cdf &a, float2 bh, float2 bl)
+__device__ __forceinline__ cdf g_cmulc2(const cdf &a, float2 bh, float2 bl, float2 C)
 {
-    return cdf_cmul2(a, make_float2(bh.x, -bh.y), make_float2(bl.x, -bl.y));
+    return g_cmul2(a, make_float2(bh.x, -bh.y), make_float2(bl.x, -bl.y), C);
 }
 
 // multiply by w16^m = exp(DIR * 2 pi i m / 16) for a compile-time m
-template <int M, int DIR> __device__ __forceinline__ cdf cdf_mulw16(const cdf &a)
+template <int M, int DIR> __device__ __forceinline__ cdf g_mulw16(const cdf &a, float2 C)
 {
     using K = DftConst<float>;
     constexpr int m = ((M % 16) + 16) % 16;
     if constexpr (m == 0) return a;
-    else if constexpr (m == 4) return cdf_muli<DIR>(a);
-    else if constexpr (m == 8) return cdf_neg(a);
-    else if constexpr (m == 12) return cdf_muli<-DIR>(a);
+    else if constexpr (m == 4) return g_muli<DIR>(a);
+    else if constexpr (m == 8) return g_neg(a);
+    else if constexpr (m == 12) return g_muli<-DIR>(a);
     else if constexpr (m % 2 == 0) {
         // odd multiple of pi/4: value = (sc + i ss) / sqrt2 with sc, ss = +-1
         constexpr int q = m / 2;
         constexpr float sc = (q == 1 || q == 7) ? 1.f : -1.f;
         constexpr float ss = ((q == 1 || q == 3) ? 1.f : -1.f) * (float)DIR;
-        // (sc ax - ss ay, ss ax + sc ay) = (sc, ss) ax + (-ss, sc) ay, exact signs
+        // (sc ax - ss ay, ss ax + sc ay) = (sc, ss) ax + (-ss, sc) ay: exact
+        // sign changes and one exact grid add, then the sqrt(1/2) product
         const cdf A{make_float2(sc * a.h.x, ss * a.h.x), make_float2(sc * a.l.x, ss * a.l.x)};
         const cdf B{make_float2(-ss * a.h.y, sc * a.h.y), make_float2(-ss * a.l.y, sc * a.l.y)};
-        return cdf_rmul2(cdf_add(A, B), K::Hh, K::Hl);
+        return g_rmul2(g_add(A, B), K::Hh, K::Hl, C);
     } else {
         constexpr int ci = (m == 1 || m == 15) ? 1 : (m == 3 || m == 13) ? 2 : (m == 5 || m == 11) ? -2 : -1;
         constexpr int si = (m == 1 || m == 7) ? 2 : (m == 3 || m == 5) ? 1 : (m == 9 || m == 15) ? -2 : -1;
@@ -199,56 +205,45 @@ template <int M, int DIR> __device__ __forceinline__ cdf cdf_mulw16(const cdf &a
         const float crl = (ci == 1 || ci == -1) ? (ci > 0 ? K::C1l : -K::C1l) : (ci > 0 ? K::S1l : -K::S1l);
         const float srh = (si == 2 || si == -2) ? (si > 0 ? K::S1h : -K::S1h) : (si > 0 ? K::C1h : -K::C1h);
         const float srl = (si == 2 || si == -2) ? (si > 0 ? K::S1l : -K::S1l) : (si > 0 ? K::C1l : -K::C1l);
-        return cdf_cmul2(a, make_float2(crh, (float)DIR * srh), make_float2(crl, (float)DIR * srl));
+        return g_cmul2(a, make_float2(crh, (float)DIR * srh), make_float2(crl, (float)DIR * srl), C);
     }
 }
 
-template <int DIR> __device__ __forceinline__ void cdf_dft2(cdf &a0, cdf &a1)
+template <int DIR> __device__ __forceinline__ void g_dft2(cdf &a0, cdf &a1)
 {
     const cdf t = a0;
-    a0 = cdf_add(t, a1);
-    a1 = cdf_sub(t, a1);
+    a0 = g_add(t, a1);
+    a1 = g_sub(t, a1);
 }
 
-template <int DIR> __device__ __forceinline__ void cdf_dft4(cdf &a0, cdf &a1, cdf &a2, cdf &a3)
+template <int DIR> __device__ __forceinline__ void g_dft4(cdf &a0, cdf &a1, cdf &a2, cdf &a3)
 {
-    const cdf s02 = cdf_add(a0, a2), d02 = cdf_sub(a0, a2);
-    const cdf s13 = cdf_add(a1, a3), t = cdf_muli<DIR>(cdf_sub(a1, a3));
-    a0 = cdf_add(s02, s13);
-    a2 = cdf_sub(s02, s13);
-    a1 = cdf_add(d02, t);
-    a3 = cdf_sub(d02, t);
-}
-// the same on FP32 inputs (lo parts zero)
-template <int DIR> __device__ __forceinline__ void cdf_dft4_0(float2 x0, float2 x1, float2 x2, float2 x3, cdf &a0,
-                                                          cdf &a1, cdf &a2, cdf &a3)
-{
-    const cdf s02 = cdf_add0(x0, x2), d02 = cdf_sub0(x0, x2);
-    const cdf s13 = cdf_add0(x1, x3), t = cdf_muli<DIR>(cdf_sub0(x1, x3));
-    a0 = cdf_add(s02, s13);
-    a2 = cdf_sub(s02, s13);
-    a1 = cdf_add(d02, t);
-    a3 = cdf_sub(d02, t);
+    const cdf s02 = g_add(a0, a2), d02 = g_sub(a0, a2);
+    const cdf s13 = g_add(a1, a3), t = g_muli<DIR>(g_sub(a1, a3));
+    a0 = g_add(s02, s13);
+    a2 = g_sub(s02, s13);
+    a1 = g_add(d02, t);
+    a3 = g_sub(d02, t);
 }
 
 // the 16-point transform after its first radix-4 level: b[j1 + 4 k1] holds
 // the inner DFT4 over j2 of x[j1 + 4 j2]; twiddles, outer DFT4s, natural order
-template <int DIR> __device__ __forceinline__ void cdf_dft16_tail(cdf *a)
+template <int DIR> __device__ __forceinline__ void g_dft16_tail(cdf *a, float2 C)
 {
-    a[5] = cdf_mulw16<1, DIR>(a[5]);
-    a[9] = cdf_mulw16<2, DIR>(a[9]);
-    a[13] = cdf_mulw16<3, DIR>(a[13]);
-    a[6] = cdf_mulw16<2, DIR>(a[6]);
-    a[10] = cdf_mulw16<4, DIR>(a[10]);
-    a[14] = cdf_mulw16<6, DIR>(a[14]);
-    a[7] = cdf_mulw16<3, DIR>(a[7]);
-    a[11] = cdf_mulw16<6, DIR>(a[11]);
-    a[15] = cdf_mulw16<9, DIR>(a[15]);
+    a[5] = g_mulw16<1, DIR>(a[5], C);
+    a[9] = g_mulw16<2, DIR>(a[9], C);
+    a[13] = g_mulw16<3, DIR>(a[13], C);
+    a[6] = g_mulw16<2, DIR>(a[6], C);
+    a[10] = g_mulw16<4, DIR>(a[10], C);
+    a[14] = g_mulw16<6, DIR>(a[14], C);
+    a[7] = g_mulw16<3, DIR>(a[7], C);
+    a[11] = g_mulw16<6, DIR>(a[11], C);
+    a[15] = g_mulw16<9, DIR>(a[15], C);
     cdf o[16];
 #pragma unroll
     for (int k1 = 0; k1 < 4; k1++) {
         cdf u0 = a[4 * k1 + 0], u1 = a[4 * k1 + 1], u2 = a[4 * k1 + 2], u3 = a[4 * k1 + 3];
-        cdf_dft4<DIR>(u0, u1, u2, u3);
+        g_dft4<DIR>(u0, u1, u2, u3);
         o[k1] = u0;
         o[k1 + 4] = u1;
         o[k1 + 8] = u2;
@@ -258,16 +253,16 @@ template <int DIR> __device__ __forceinline__ void cdf_dft16_tail(cdf *a)
     for (int i = 0; i < 16; i++) a[i] = o[i];
 }
 
-template <int DIR> __device__ __forceinline__ void cdf_dft8_tail(cdf *a)
+template <int DIR> __device__ __forceinline__ void g_dft8_tail(cdf *a, float2 C)
 {
-    a[3] = cdf_mulw16<2, DIR>(a[3]);
-    a[5] = cdf_mulw16<4, DIR>(a[5]);
-    a[7] = cdf_mulw16<6, DIR>(a[7]);
+    a[3] = g_mulw16<2, DIR>(a[3], C);
+    a[5] = g_mulw16<4, DIR>(a[5], C);
+    a[7] = g_mulw16<6, DIR>(a[7], C);
     cdf o[8];
 #pragma unroll
     for (int k1 = 0; k1 < 4; k1++) {
         cdf u0 = a[2 * k1], u1 = a[2 * k1 + 1];
-        cdf_dft2<DIR>(u0, u1);
+        g_dft2<DIR>(u0, u1);
         o[k1] = u0;
         o[k1 + 4] = u1;
     }
@@ -275,47 +270,24 @@ template <int DIR> __device__ __forceinline__ void cdf_dft8_tail(cdf *a)
     for (int i = 0; i < 8; i++) a[i] = o[i];
 }
 
-// In-place natural-order DFT of size N (1, 2, 4, 8, 16) on double-float values.
-template <int N, int DIR> __device__ __forceinline__ void cdf_dft(cdf *a)
+// In-place natural-order DFT of size N (1, 2, 4, 8, 16) on gridded values
+// (every h a multiple of the quantum of C).
+template <int N, int DIR> __device__ __forceinline__ void g_dft(cdf *a, float2 C)
 {
     if constexpr (N == 2) {
-        cdf_dft2<DIR>(a[0], a[1]);
+        g_dft2<DIR>(a[0], a[1]);
     } else if constexpr (N == 4) {
-        cdf_dft4<DIR>(a[0], a[1], a[2], a[3]);
+        g_dft4<DIR>(a[0], a[1], a[2], a[3]);
     } else if constexpr (N == 8) {
-        cdf_dft4<DIR>(a[0], a[2], a[4], a[6]);
-        cdf_dft4<DIR>(a[1], a[3], a[5], a[7]);
-        cdf_dft8_tail<DIR>(a);
+        g_dft4<DIR>(a[0], a[2], a[4], a[6]);
+        g_dft4<DIR>(a[1], a[3], a[5], a[7]);
+        g_dft8_tail<DIR>(a, C);
     } else if constexpr (N == 16) {
-        cdf_dft4<DIR>(a[0], a[4], a[8], a[12]);
-        cdf_dft4<DIR>(a[1], a[5], a[9], a[13]);
-        cdf_dft4<DIR>(a[2], a[6], a[10], a[14]);
-        cdf_dft4<DIR>(a[3], a[7], a[11], a[15]);
-        cdf_dft16_tail<DIR>(a);
-    }
-}
-
-// The same transform of FP32 inputs x[0..N) into double-float outputs a[0..N)
-// (the first level needs no lo parts).
-template <int N, int DIR> __device__ __forceinline__ void cdf_dft_from(const float2 *x, cdf *a)
-{
-    if constexpr (N == 1) {
-        a[0] = c_of(x[0]);
-    } else if constexpr (N == 2) {
-        a[0] = cdf_add0(x[0], x[1]);
-        a[1] = cdf_sub0(x[0], x[1]);
-    } else if constexpr (N == 4) {
-        cdf_dft4_0<DIR>(x[0], x[1], x[2], x[3], a[0], a[1], a[2], a[3]);
-    } else if constexpr (N == 8) {
-        cdf_dft4_0<DIR>(x[0], x[2], x[4], x[6], a[0], a[2], a[4], a[6]);
-        cdf_dft4_0<DIR>(x[1], x[3], x[5], x[7], a[1], a[3], a[5], a[7]);
-        cdf_dft8_tail<DIR>(a);
-    } else if constexpr (N == 16) {
-        cdf_dft4_0<DIR>(x[0], x[4], x[8], x[12], a[0], a[4], a[8], a[12]);
-        cdf_dft4_0<DIR>(x[1], x[5], x[9], x[13], a[1], a[5], a[9], a[13]);
-        cdf_dft4_0<DIR>(x[2], x[6], x[10], x[14], a[2], a[6], a[10], a[14]);
-        cdf_dft4_0<DIR>(x[3], x[7], x[11], x[15], a[3], a[7], a[11], a[15]);
-        cdf_dft16_tail<DIR>(a);
+        g_dft4<DIR>(a[0], a[4], a[8], a[12]);
+        g_dft4<DIR>(a[1], a[5], a[9], a[13]);
+        g_dft4<DIR>(a[2], a[6], a[10], a[14]);
+        g_dft4<DIR>(a[3], a[7], a[11], a[15]);
+        g_dft16_tail<DIR>(a, C);
     }
 }
 

@@ -253,9 +253,6 @@ template <typename T, bool XL, int FEAT = 0> struct PassGeom {
 #endif
 // Compensated passes (FEAT_COMP) hold every transform value as hi + lo: 512
 // threads per SM (128 registers).
-#ifndef GPSS_COMP_PHASE_PLAIN
-#define GPSS_COMP_PHASE_PLAIN 0
-#endif
 #ifndef GPSS_PASS_SM_THREADS_COMP_F32
 #define GPSS_PASS_SM_THREADS_COMP_F32 512
 #endif
@@ -529,43 +526,62 @@ pass_kernel(const PassArgs<T> a)
     if constexpr (kTopBarrier) line_sync();  // the previous tile's stage B is done with sdata
 
     if constexpr (kComp) {
-        // compensated kinetic pass: the same stages on double-float values
+        // compensated kinetic pass: the same stages on gridded two-float
+        // values (fft_comp.cuh); each thread grids each stage's values on its
+        // own quantum.  The deferred factor enters with the first gridding
+        // (an exact product and residual), which is the same linear map as
+        // scaling the spectrum.
         cdf c[N1];
-        cdf_dft_from<N1, -1>(v, c);
-        if constexpr (N2 == 1) {
-            if (red & RED_KIN) {
-                T s2 = 0, s1 = 0;
+        {
+            const float sc = tscaled ? (float)tscale : 1.f;
+            const float2 C = grid_for(absmax<N1>(v) * fabsf(sc));
+            if (tscaled) {
+                const float2 S = make_float2(sc, sc);
+#pragma unroll
+                for (int j = 0; j < N1; j++) c[j] = g_from_scaled(v[j], S, C);
+            } else {
+#pragma unroll
+                for (int j = 0; j < N1; j++) c[j] = g_from(v[j], C);
+            }
+            g_dft<N1, -1>(c, C);
+            if constexpr (N2 == 1) {
+                if (red & RED_KIN) {
+                    T s2 = 0, s1 = 0;
+#pragma unroll
+                    for (int k = 0; k < N1; k++) {
+                        const int kk = k < N / 2 ? k : k - N;
+                        const T xi = (T)kk * kmult;
+                        const float2 X = c_round(c[k]);
+                        const T m2 = X.x * X.x + X.y * X.y;
+                        s2 += xi * xi * m2;
+                        s1 += xi * m2;
+                    }
+                    acc_kin += s2 * (T)(1.0 / N);
+                    if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
+                }
 #pragma unroll
                 for (int k = 0; k < N1; k++) {
-                    const int kk = k < N / 2 ? k : k - N;
-                    const T xi = (T)kk * kmult;
-                    const T m2 = c[k].h.x * c[k].h.x + c[k].h.y * c[k].h.y;
-                    s2 += xi * xi * m2;
-                    s1 += xi * m2;
+                    const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
+                                              : sph[k];
+                    c[k] = g_cmul2(c[k], p.hi, p.lo, C);
                 }
-                acc_kin += s2 * (T)(1.0 / N);
-                if (a.coord) acc_rot += s1 * (T)(1.0 / N) * (T)a.coord[row];
-            }
+                g_dft<N1, +1>(c, C);
+            } else {
+                // stage A store: (k1, r) <- c[k1] * w_n^{r k1}, h and l
 #pragma unroll
-            for (int k = 0; k < N1; k++) {
-                const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]} : sph[k];
-                c[k] = cdf_cmul2(c[k], p.hi, p.lo);
-                if (tscaled) c[k] = cdf_scale(c[k], tscale);
-            }
-            cdf_dft<N1, +1>(c);
-        } else {
-            // stage A store: (k1, r) <- c[k1] * w_n^{r k1}, hi and lo
-#pragma unroll
-            for (int k1 = 0; k1 < N1; k1++) {
-                const int m = k1 * N2 + r;
-                cdf t = c[k1];
-                if (k1 != 0 && r != 0) {
-                    const DWord<V> w2 = stw[m];
-                    t = cdf_cmul2(t, w2.hi, w2.lo);
+                for (int k1 = 0; k1 < N1; k1++) {
+                    const int m = k1 * N2 + r;
+                    cdf t = c[k1];
+                    if (k1 != 0 && r != 0) {
+                        const DWord<V> w2 = stw[m];
+                        t = g_cmul2(t, w2.hi, w2.lo, C);
+                    }
+                    sdata[sidx(m)] = t.h;
+                    slo[sidx(m)] = t.l;
                 }
-                sdata[sidx(m)] = t.h;
-                slo[sidx(m)] = t.l;
             }
+        }
+        if constexpr (N2 > 1) {
             line_sync();
             constexpr int NI = N1 / N2;
 #pragma unroll
@@ -577,7 +593,10 @@ pass_kernel(const PassArgs<T> a)
                     u[rr].h = sdata[sidx(k1 * N2 + rr)];
                     u[rr].l = slo[sidx(k1 * N2 + rr)];
                 }
-                cdf_dft<N2, -1>(u);  // u[k2] = X[k1 + N1 k2]
+                const float2 C = grid_for(absmax<N2>(u));
+#pragma unroll
+                for (int rr = 0; rr < N2; rr++) u[rr] = g_regrid(u[rr], C);
+                g_dft<N2, -1>(u, C);  // u[k2] = X[k1 + N1 k2]
                 if (red & RED_KIN) {
                     T s2 = 0, s1 = 0;
 #pragma unroll
@@ -585,7 +604,8 @@ pass_kernel(const PassArgs<T> a)
                         const int k = k1 + N1 * k2;
                         const int kk = k < N / 2 ? k : k - N;
                         const T xi = (T)kk * kmult;
-                        const T m2 = u[k2].h.x * u[k2].h.x + u[k2].h.y * u[k2].h.y;
+                        const float2 X = c_round(u[k2]);
+                        const T m2 = X.x * X.x + X.y * X.y;
                         s2 += xi * xi * m2;
                         s1 += xi * m2;
                     }
@@ -597,21 +617,15 @@ pass_kernel(const PassArgs<T> a)
                     const int k = k1 + N1 * k2;
                     const DWord<V> p = prow ? DWord<V>{a.phase[row * prow + k], a.phase[row * prow + N + k]}
                                               : sph[k];
-#if GPSS_COMP_PHASE_PLAIN
-                    u[k2].h = cmul2(u[k2].h, p.hi, p.lo);
-                    u[k2].l = cmul(u[k2].l, p.hi);
-#else
-                    u[k2] = cdf_cmul2(u[k2], p.hi, p.lo);
-#endif
-                    if (tscaled) u[k2] = cdf_scale(u[k2], tscale);
+                    u[k2] = g_cmul2(u[k2], p.hi, p.lo, C);
                 }
-                cdf_dft<N2, +1>(u);
+                g_dft<N2, +1>(u, C);
 #pragma unroll
                 for (int rr = 0; rr < N2; rr++) {
                     cdf t = u[rr];
                     if (k1 != 0 && rr != 0) {
                         const DWord<V> w2 = stwB[rr * N1 + k1];
-                        t = cdf_cmulc2(t, w2.hi, w2.lo);
+                        t = g_cmulc2(t, w2.hi, w2.lo, C);
                     }
                     sdata[sidx(k1 * N2 + rr)] = t.h;
                     slo[sidx(k1 * N2 + rr)] = t.l;
@@ -623,7 +637,10 @@ pass_kernel(const PassArgs<T> a)
                 c[k1].h = sdata[sidx(k1 * N2 + r)];
                 c[k1].l = slo[sidx(k1 * N2 + r)];
             }
-            cdf_dft<N1, +1>(c);
+            const float2 C = grid_for(absmax<N1>(c));
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) c[k1] = g_regrid(c[k1], C);
+            g_dft<N1, +1>(c, C);
         }
 #pragma unroll
         for (int j = 0; j < N1; j++) v[j] = c_round(c[j]);
