@@ -234,10 +234,15 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #ifndef GPSS_PASS_THREADS_COL_LEAN_F32
 #define GPSS_PASS_THREADS_COL_LEAN_F32 256
 #endif
+// compensated y/z passes: CTAs of this many threads
+#ifndef GPSS_PASS_THREADS_COL_COMP_F32
+#define GPSS_PASS_THREADS_COL_COMP_F32 256
+#endif
 template <typename T, bool XL, int FEAT = 0> struct PassGeom {
     static constexpr int THREADS =
         sizeof(T) == 4 ? (XL ? GPSS_PASS_THREADS_XL_F32
                              : ((FEAT & FEAT_SMALL) ? 128
+                                : (FEAT & FEAT_COMP) ? GPSS_PASS_THREADS_COL_COMP_F32
                                 : (FEAT == FEAT_NONE ? GPSS_PASS_THREADS_COL_LEAN_F32 : GPSS_PASS_THREADS_COL_F32)))
                        : GPSS_PASS_THREADS_F64;
 };
