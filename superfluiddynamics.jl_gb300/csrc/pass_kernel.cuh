@@ -234,9 +234,13 @@ template <typename V> struct __align__(2 * sizeof(V)) DWord {
 #ifndef GPSS_PASS_THREADS_COL_LEAN_F32
 #define GPSS_PASS_THREADS_COL_LEAN_F32 256
 #endif
-// compensated y/z passes: CTAs of this many threads
+// compensated y/z passes: CTAs of 128 threads (8 columns, 64 B runs), four
+// per SM: fewer threads wait at each of the two stage barriers (256^3: y
+// 152.3 -> 146.6 us, z+NL 159.4 -> 157.2 us against 256-thread CTAs).  Their
+// tile count, cells / 2048, is that of the 128-thread x pass, which the
+// context's partial-sum buffer already holds.
 #ifndef GPSS_PASS_THREADS_COL_COMP_F32
-#define GPSS_PASS_THREADS_COL_COMP_F32 256
+#define GPSS_PASS_THREADS_COL_COMP_F32 128
 #endif
 template <typename T, bool XL, int FEAT = 0> struct PassGeom {
     static constexpr int THREADS =
