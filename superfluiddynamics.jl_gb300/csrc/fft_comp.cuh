@@ -152,54 +152,27 @@ __device__ __forceinline__ cdf g_neg(const cdf &a) { return cdf{p_neg(a.h), p_ne
 __device__ __forceinline__ cdf g_rmul2(const cdf &a, float hi, float lo, float2 C)
 {
     const float2 H = make_float2(hi, hi), L = make_float2(lo, lo);
-#if GPSS_COMP_VARIANT & 1
-    const float2 s = p_fma(a.h, H, C);
-    const float2 nh = p_sub(C, s);
-    const float2 r = p_fma(a.h, H, nh);
-    const float2 h = p_sub(s, C);
-#else
     const float2 h = p_sub(p_fma(a.h, H, C), C);
     const float2 r = p_fma(a.h, H, p_neg(h));
-#endif
     return cdf{h, p_fma(a.h, L, p_fma(a.l, H, r))};
 }
 
 // a * (bh + bl), b a double-word complex constant, as packed pairs:
 //   (re, im) = (ax, ax) * (bx, by) + (ay, ay) * (-by, bx)
 // each of the two packed products is gridded with its exact residual
-#ifndef GPSS_COMP_VARIANT
-#define GPSS_COMP_VARIANT 0
-#endif
 __device__ __forceinline__ cdf g_cmul2(const cdf &a, float2 bh, float2 bl, float2 C)
 {
     const float2 X = make_float2(a.h.x, a.h.x), Y = make_float2(a.h.y, a.h.y);
     const float2 b2 = make_float2(-bh.y, bh.x), bl2 = make_float2(-bl.y, bl.x);
-#if GPSS_COMP_VARIANT & 1
-    // residuals against -u = C - s, so no operand needs a negation
-    const float2 s1 = p_fma(X, bh, C), s2 = p_fma(Y, b2, C);
-    const float2 nu = p_sub(C, s1), nv = p_sub(C, s2);
-    const float2 r1 = p_fma(X, bh, nu), r2 = p_fma(Y, b2, nv);
-    const float2 h = p_sub(p_sub(s1, C), nv);
-#else
     const float2 u = p_sub(p_fma(X, bh, C), C);
     const float2 v = p_sub(p_fma(Y, b2, C), C);
-    const float2 r1 = p_fma(X, bh, p_neg(u)), r2 = p_fma(Y, b2, p_neg(v));
-    const float2 h = p_add(u, v);
-#endif
-#if GPSS_COMP_VARIANT & 2
-    // two independent accumulation chains
-    float2 l1 = p_fma(X, bl, r1), l2 = p_fma(Y, bl2, r2);
+    // the low parts in two independent chains (2% faster at 256^3 than one
+    // chain; residual forms without the negated operands were 5% slower)
+    float2 l1 = p_fma(X, bl, p_fma(X, bh, p_neg(u)));
+    float2 l2 = p_fma(Y, bl2, p_fma(Y, b2, p_neg(v)));
     l1 = p_fma(make_float2(a.l.x, a.l.x), bh, l1);
     l2 = p_fma(make_float2(a.l.y, a.l.y), b2, l2);
-    return cdf{h, p_add(l1, l2)};
-#else
-    float2 l = p_add(r1, r2);
-    l = p_fma(X, bl, l);
-    l = p_fma(Y, bl2, l);
-    l = p_fma(make_float2(a.l.x, a.l.x), bh, l);
-    l = p_fma(make_float2(a.l.y, a.l.y), b2, l);
-    return cdf{h, l};
-#endif
+    return cdf{p_add(u, v), p_add(l1, l2)};
 }
 // a * conj(bh + bl)
 __device__ __forceinline__ cdf g_cmulc2(const cdf &a, float2 bh, float2 bl, float2 C)
