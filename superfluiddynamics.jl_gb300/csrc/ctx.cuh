@@ -427,6 +427,10 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
         GPSS_TRY(get_phase(c, axis, dtl, imag, 1, &ph, &a.prow));
         a.phase = (const vec2<T> *)ph;
         a.comp = sizeof(T) == 4 && (c->flags & GPSS_FLAG_COMPENSATED) != 0;
+        // the FP32 mass lock holds the field at the target mass M0 (its
+        // diagnostics slot) through the call: the compensated passes grid on
+        // a bound from it
+        if (a.comp && fin_last == FIN_MASSLOCK) a.grid_mass = c->sums + kDiagSlot * RQ_COUNT + RQ_MASS;
         if (prescale && step == 0) a.scale = c->scale;
         const bool last = step == c->ndim - 1;
         if (last && nl) {

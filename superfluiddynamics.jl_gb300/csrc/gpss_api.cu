@@ -745,6 +745,10 @@ int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double 
         GPSS_TRY(get_phase(c, axis, dt, 0, 1, &ph, &a.prow));
         a.phase = (const vec2<T> *)ph;
         a.comp = sizeof(T) == 4 && (c->flags & GPSS_FLAG_COMPENSATED) != 0;
+        if (a.comp) {  // the mass bound of the real-time passes (the mass-lock target slot)
+            GPSS_TRY(diag_passes<T>(c, false, FIN_NONE));
+            a.grid_mass = c->sums + kDiagSlot * RQ_COUNT + RQ_MASS;
+        }
         if (mode == 1) {
             a.nl_mode = NL_REAL;
             a.V = c->have_V ? (const T *)c->V : nullptr;

@@ -178,6 +178,13 @@ template <typename T> struct PassArgs {
     const int *mask_lim;
     // FP32 FUSED passes: nonzero selects the compensated instantiation (FEAT_COMP)
     int comp;
+    // compensated passes: nullable device pointer to a mass M >= sum |psi|^2
+    // of the pass input (after its deferred factor).  Every intermediate of a
+    // length-n transform is a sum of at most n unit-weighted values, so its
+    // modulus is at most sqrt(n M) <= 16 sqrt(M); with 2 M that bounds all
+    // stages of all lines, and one quantum for the whole pass replaces the
+    // per-thread, per-stage ones (no re-gridding between stages)
+    const double *grid_mass;
     // pipelined pass: 0 waits up to the default number of polls for a tile;
     // v > 0 waits v - 1 polls (host-side fault injection of a timeout)
     unsigned wait_polls;
@@ -449,6 +456,14 @@ pass_kernel(const PassArgs<T> a)
     const bool scaled = a.scale != nullptr;
     const T scale = scaled ? load_scale<T>(a.scale) : (T)1;
     const T kmult = a.kmult;
+    // compensated passes with a mass bound: one grid for every stage (C of
+    // the quantum 2^-22 of 32 sqrt(M/2) = 16 sqrt(2 M), rounded up)
+    const bool gridm = kComp && a.grid_mass != nullptr;
+    float2 Cm = make_float2(0.f, 0.f);
+    if constexpr (kComp) {
+        if (gridm) Cm = grid_for((float)sqrt(0.5 * *a.grid_mass));
+    }
+    (void)Cm;
 
     // accumulators: the field precision within a tile (its own cells), FP64
     // across the tiles of the CTA (one FP64 add per tile and quantity, so no
@@ -543,7 +558,7 @@ pass_kernel(const PassArgs<T> a)
         cdf c[N1];
         {
             const float sc = tscaled ? (float)tscale : 1.f;
-            const float2 C = grid_for(absmax<N1>(v) * fabsf(sc));
+            const float2 C = gridm ? Cm : grid_for(absmax<N1>(v) * fabsf(sc));
             if (tscaled) {
                 const float2 S = make_float2(sc, sc);
 #pragma unroll
@@ -602,9 +617,12 @@ pass_kernel(const PassArgs<T> a)
                     u[rr].h = sdata[sidx(k1 * N2 + rr)];
                     u[rr].l = slo[sidx(k1 * N2 + rr)];
                 }
-                const float2 C = grid_for(absmax<N2>(u));
+                float2 C = Cm;
+                if (!gridm) {
+                    C = grid_for(absmax<N2>(u));
 #pragma unroll
-                for (int rr = 0; rr < N2; rr++) u[rr] = g_regrid(u[rr], C);
+                    for (int rr = 0; rr < N2; rr++) u[rr] = g_regrid(u[rr], C);
+                }
                 g_dft<N2, -1>(u, C);  // u[k2] = X[k1 + N1 k2]
                 if (red & RED_KIN) {
                     T s2 = 0, s1 = 0;
@@ -646,9 +664,12 @@ pass_kernel(const PassArgs<T> a)
                 c[k1].h = sdata[sidx(k1 * N2 + r)];
                 c[k1].l = slo[sidx(k1 * N2 + r)];
             }
-            const float2 C = grid_for(absmax<N1>(c));
+            float2 C = Cm;
+            if (!gridm) {
+                C = grid_for(absmax<N1>(c));
 #pragma unroll
-            for (int k1 = 0; k1 < N1; k1++) c[k1] = g_regrid(c[k1], C);
+                for (int k1 = 0; k1 < N1; k1++) c[k1] = g_regrid(c[k1], C);
+            }
             g_dft<N1, +1>(c, C);
         }
 #pragma unroll
