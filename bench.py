@@ -189,6 +189,17 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
+# FP32 operations (lanes of packed f32x2 instructions; an FMA counts once) that
+# a compensated 256-point pass executes per cell, counted from fft_comp.cuh:
+# per cell 3 (onto the grid) + 4 x 12.75 (DFT-16: 8 radix-4 butterflies of
+# 8 two-word adds, 3 general and 4 sqrt(1/2) products per 16 cells) + 2 x
+# 10.55 (twiddle products, 225 of 256 cells) + 12 (phase) + 1 (rounding)
+# = 88.1 packed instructions; and ~24 for the nonlinear step and mass sum of
+# the last pass of a time step.
+COMP_OPS_PER_CELL_PASS = 2 * 88.1
+NL_OPS_PER_CELL = 24
+
+
 def profiled_traffic(kernel_tag):
     """dram bytes per launch of the dominant kernel from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
@@ -666,8 +677,8 @@ def run_gpss(args, rank, world, local):
     per_axis = pass_times(h)
     roof = roofline(per_axis, "fp32c" if comp else "fp32", t_ms / args.steps)
     if comp:
-        roof["note"] += ("; the compensated passes are bound by the FP32 pipe (double-float arithmetic, "
-                         "see profiles/), not by HBM")
+        roof["note"] += ("; the compensated passes are bound by the FMA pipe (grid-exact two-float "
+                         "arithmetic), not by HBM: see compute_fp32_pipe and profiles/")
 
     # ---- end to end through the public API with host buffers
     nbytes = int(cells) * 16
@@ -741,9 +752,24 @@ def run_gpss(args, rank, world, local):
         roof["compute"] = {"unit": "TFLOP/s", "algorithmic_flops_per_cell_step": flops_merged,
                            "achieved": ach, "fp32_fma_peak_measured": peaks["fp32_tflops"],
                            "frac": ach / peaks["fp32_tflops"],
-                           "note": "algorithmic flops of the merged step; the compensated arithmetic executes "
-                                   "several times more FP32 operations than that count (the FMA-pipe "
-                                   "utilisation from ncu is in profiles/)"}
+                           "note": "textbook FFT flops of the merged step (5 n log2 n per transform)"}
+        if comp and args.n == 256:
+            # the compensated passes are bound by the FMA pipe: their executed
+            # FP32 operations (each lane of a packed f32x2 instruction counted,
+            # an FMA counted once) against the measured FMA rate in the same
+            # unit (FMA/s = FLOP/s / 2)
+            peak_ops = peaks["fp32_tflops"] / 2
+            xo = COMP_OPS_PER_CELL_PASS * cells / (per_axis["x"] * 1e-3) / 1e12
+            so = (PASSES_PER_TIMESTEP * COMP_OPS_PER_CELL_PASS + NL_OPS_PER_CELL) * value / world * 1e6 / 1e12
+            roof["compute_fp32_pipe"] = {
+                "unit": "T FP32 ops/s", "peak": peak_ops,
+                "peak_source": "gpss_measure_fma_rate (FP32 FMA chains, CUDA events)",
+                "ops_per_cell_per_pass": COMP_OPS_PER_CELL_PASS, "nl_ops_per_cell": NL_OPS_PER_CELL,
+                "x_pass_achieved": xo, "x_pass_frac": xo / peak_ops,
+                "whole_step_achieved": so, "whole_step_frac": so / peak_ops,
+                "note": "FP32 operations the compensated 256-point pass executes per cell (88.1 packed "
+                        "f32x2 instructions: entering the grid 3, four DFT-16 51, two twiddles 21.1, "
+                        "phase 12, final rounding 1); the x pass carries no nonlinear epilogue"}
 
     # ---- FP64 plain kernels on the same workload (fewer time steps)
     fp64 = None
