@@ -85,6 +85,10 @@ static cudaError_t launch_comp_mode(const PassArgs<float> &a, int blocks, cudaSt
     const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0;
     const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
     if (diag) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_ALL>(a, blocks, s);
+    if (a.grid_mass) {  // one grid per pass from the mass bound
+        if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_GRIDM | FEAT_NL>(a, blocks, s);
+        return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_GRIDM>(a, blocks, s);
+    }
     if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_NL>(a, blocks, s);
     return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP>(a, blocks, s);
 }

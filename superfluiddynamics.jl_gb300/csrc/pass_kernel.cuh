@@ -89,11 +89,14 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //   FEAT_ACC   the `acc` epilogue alone (add the result to a second field:
 //              the y/z passes of lapRot in the RK and implicit schemes)
 //   FEAT_COMP  (FP32) compensated arithmetic: the transforms, twiddles and
-//              phase run on double-float values (fft_comp.cuh), so the only
-//              FP32 rounding of the pass is the store; combined with
+//              phase run on grid-exact two-float values (fft_comp.cuh), so
+//              the only FP32 rounding of the pass is the store; combined with
 //              FEAT_NONE, FEAT_NL or FEAT_ALL
+//   FEAT_GRIDM (with FEAT_COMP, without FEAT_DIAG) one grid for the whole
+//              pass from the mass bound `grid_mass` instead of a grid per
+//              thread and stage (no re-gridding between stages)
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
-       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128, FEAT_COMP = 256 };
+       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128, FEAT_COMP = 256, FEAT_GRIDM = 512 };
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -458,11 +461,9 @@ pass_kernel(const PassArgs<T> a)
     const T kmult = a.kmult;
     // compensated passes with a mass bound: one grid for every stage (C of
     // the quantum 2^-22 of 32 sqrt(M/2) = 16 sqrt(2 M), rounded up)
-    const bool gridm = kComp && a.grid_mass != nullptr;
+    constexpr bool gridm = kComp && (FEAT & FEAT_GRIDM) != 0;
     float2 Cm = make_float2(0.f, 0.f);
-    if constexpr (kComp) {
-        if (gridm) Cm = grid_for((float)sqrt(0.5 * *a.grid_mass));
-    }
+    if constexpr (gridm) Cm = grid_for((float)sqrt(0.5 * *a.grid_mass));
     (void)Cm;
 
     // accumulators: the field precision within a tile (its own cells), FP64
@@ -618,7 +619,7 @@ pass_kernel(const PassArgs<T> a)
                     u[rr].l = slo[sidx(k1 * N2 + rr)];
                 }
                 float2 C = Cm;
-                if (!gridm) {
+                if constexpr (!gridm) {
                     C = grid_for(absmax<N2>(u));
 #pragma unroll
                     for (int rr = 0; rr < N2; rr++) u[rr] = g_regrid(u[rr], C);
@@ -665,7 +666,7 @@ pass_kernel(const PassArgs<T> a)
                 c[k1].l = slo[sidx(k1 * N2 + r)];
             }
             float2 C = Cm;
-            if (!gridm) {
+            if constexpr (!gridm) {
                 C = grid_for(absmax<N1>(c));
 #pragma unroll
                 for (int k1 = 0; k1 < N1; k1++) c[k1] = g_regrid(c[k1], C);
