@@ -92,3 +92,19 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 }
 
 }  // namespace gpss
+
+namespace gpss {
+
+// tensor (TMA) load of a 3D box into shared memory, completing `bytes` of the
+// barrier's transaction count; `tmap` is a CUtensorMap in global memory
+// (64-byte aligned), coordinates are element indices, innermost first
+__device__ __forceinline__ void tma_load_3d(void *dst_smem, const void *tmap, int c0, int c1, int c2, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst_smem)),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+}  // namespace gpss

@@ -13,6 +13,7 @@
 #include <new>
 #include <string>
 #include <nvtx3/nvToolsExt.h>
+#include <cuda.h>
 #include "../../include/gpss.h"
 #include "gpss_internal.h"
 
@@ -66,6 +67,9 @@ struct gpss_ctx {
     std::vector<double> coord[3];
     double *partials = nullptr;
     int max_blocks = 0;
+    // FP32 3D fields: tensor maps of psi for the y and z passes' tile copies
+    // (two CUtensorMap, 64-byte aligned, in device memory); null if unused
+    void *tmap_dev = nullptr;
     double *sums = nullptr;   // [4][RQ_COUNT]: slots 0..2 per axis, slot 3 diagnostics
     double *scale = nullptr;  // ScaleCell: the factor in FP64 and as a float
     int *status = nullptr;    // [1]
@@ -431,6 +435,16 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
         // diagnostics slot) through the call: the compensated passes grid on
         // a bound from it
         if (a.comp && fin_last == FIN_MASSLOCK) a.grid_mass = c->sums + kDiagSlot * RQ_COUNT + RQ_MASS;
+        // plain FP32 y/z passes of psi under the mass lock (the call checks
+        // the status word, where a tile copy that timed out is reported):
+        // tiles arrive by tensor copies
+        if (c->tmap_dev && !a.comp && axis >= 1 && field == c->psi && fin_last == FIN_MASSLOCK && !diag_kin &&
+            a.prow == 0) {
+            a.tmap = (const char *)c->tmap_dev + (axis - 1) * sizeof(CUtensorMap);
+            a.taxis = axis;
+            a.tnx = (int)c->n[0];
+            a.fin_status = c->status;
+        }
         if (prescale && step == 0) a.scale = c->scale;
         const bool last = step == c->ndim - 1;
         if (last && nl) {

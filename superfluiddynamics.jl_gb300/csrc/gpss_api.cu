@@ -1,6 +1,7 @@
 // gpss_api.cu -- the C ABI of libgpss.so (include/gpss.h): context setup,
 // host-built FP64 tables, and the orchestration of the directional passes
 // that make up NumModelSplit1 / NumModelSplit2 time steps.
+#include <cuda.h>
 #include "ctx.cuh"
 
 static thread_local std::string g_create_error;
@@ -158,6 +159,50 @@ template <typename T> static int imag_merged(gpss_ctx *c, int nsteps, double dt)
 }
 
 // the cached energies of the current field (GPSS_FLAG_ENERGY_CACHE), if any
+// Tensor maps for the FEAT_TMA y/z passes of an FP32 3D field: psi as a
+// (nx, ny, nz) tensor of 8-byte elements, boxes of W x-adjacent columns by a
+// whole line (W = the pass's lines per CTA, which must divide nx).  The
+// encoder comes from the driver through the runtime's entry-point query, so
+// the library links no driver library.  No map (a plain loads pass) when the
+// shapes do not fit or the query fails.
+#ifndef GPSS_PASS_TMA
+#define GPSS_PASS_TMA 1
+#endif
+static int make_tensor_maps(gpss_ctx *c)
+{
+    if (!GPSS_PASS_TMA || c->precision != GPSS_FP32 || c->ndim != 3 || any_generic(c)) return GPSS_OK;
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return GPSS_OK;
+    }
+    CUtensorMap maps[2];
+    std::memset(maps, 0, sizeof(maps));
+    const cuuint64_t dims[3] = {(cuuint64_t)c->n[0], (cuuint64_t)c->n[1], (cuuint64_t)c->n[2]};
+    const cuuint64_t strides[2] = {(cuuint64_t)c->n[0] * 8, (cuuint64_t)(c->n[0] * c->n[1]) * 8};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    for (int axis = 1; axis <= 2; axis++) {
+        const int64_t n = c->n[axis];
+        const int W = PassLauncher<float>::lines((int)n, false);
+        if (n < 64 || W < 2 || c->n[0] % W) return GPSS_OK;
+        const cuuint32_t box[3] = {(cuuint32_t)W, axis == 1 ? (cuuint32_t)n : 1u, axis == 2 ? (cuuint32_t)n : 1u};
+        const CUresult r = reinterpret_cast<EncodeFn>(fn)(
+            &maps[axis - 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, c->psi, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return GPSS_OK;
+    }
+    GPSS_TRY(dev_alloc(c, &c->tmap_dev, sizeof(maps)));
+    CUDA_TRY(c, cudaMemcpy(c->tmap_dev, maps, sizeof(maps), cudaMemcpyHostToDevice));
+    return GPSS_OK;
+}
+
 static bool ecache_fresh(const gpss_ctx *c)
 {
     return (c->flags & GPSS_FLAG_ENERGY_CACHE) && c->ecache_version == c->version;
@@ -342,7 +387,7 @@ void gpss_destroy(gpss_ctx *c)
     void *ptrs[] = {c->psi, c->scratch, c->V, c->tw[0], c->tw[1], c->tw[2], c->coord_dev[0],
                     c->coord_dev[1], c->coord_dev[2], c->partials, c->sums, c->scale, c->status,
                     c->counter, c->rk_buf[0], c->rk_buf[1], c->rk_buf[2], c->rk_buf[3], c->rk_lim,
-                    c->adj_buf, c->im_buf};
+                    c->adj_buf, c->im_buf, c->tmap_dev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : c->ev)
@@ -456,6 +501,7 @@ int gpss_create(gpss_ctx **out, int ndim, const int64_t *n, const double *lo, co
     if ((rc = dev_alloc(c, (void **)&c->scale, sizeof(double) * 2))) return bail(rc);
     if ((rc = dev_alloc(c, (void **)&c->status, sizeof(int) * 2))) return bail(rc);
     if ((rc = dev_alloc(c, (void **)&c->counter, sizeof(unsigned int) * 2))) return bail(rc);
+    if ((rc = make_tensor_maps(c))) return bail(rc);
     e = cudaHostAlloc((void **)&c->host_stage, sizeof(double) * (4 * RQ_COUNT + 1), cudaHostAllocDefault);
     if (e != cudaSuccess) {
         c->host_stage = nullptr;
@@ -748,6 +794,12 @@ int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double 
         if (a.comp) {  // the mass bound of the real-time passes (the mass-lock target slot)
             GPSS_TRY(diag_passes<T>(c, false, FIN_NONE));
             a.grid_mass = c->sums + kDiagSlot * RQ_COUNT + RQ_MASS;
+        } else if (c->tmap_dev && axis >= 1) {  // the tensor-copy tiles of the real-time y/z passes
+            a.tmap = (const char *)c->tmap_dev + (axis - 1) * sizeof(CUtensorMap);
+            a.taxis = axis;
+            a.tnx = (int)c->n[0];
+            a.fin_status = c->status;
+            CUDA_TRY(c, cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
         }
         if (mode == 1) {
             a.nl_mode = NL_REAL;

@@ -122,6 +122,13 @@ static cudaError_t launch_pass_mode(int mode, const PassArgs<T> &a, int blocks, 
                 return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_PLANE>(a, blocks, s);
             }
         }
+        if constexpr (sizeof(T) == 4 && !XL && N >= 64) {
+            // y/z columns of a 3D field with a tensor map: tiles arrive by TMA
+            if (a.tmap && !diag && !acc && !adj) {
+                if (nl) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_TMA | FEAT_NL>(a, blocks, s);
+                return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_TMA>(a, blocks, s);
+            }
+        }
         if (diag || (acc && (adj || nl))) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ALL>(a, blocks, s);
         if (acc) return launch_pass_inst<T, N, XL, MODE_FUSED, FEAT_ACC>(a, blocks, s);
         if constexpr (sizeof(T) == 4 && !XL && N >= 64) {

@@ -46,6 +46,7 @@
 #include "fft_core.cuh"
 #include "fft_comp.cuh"
 #include "nl_phase.cuh"
+#include "bulk_async.cuh"
 
 namespace gpss {
 
@@ -95,8 +96,15 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //   FEAT_GRIDM (with FEAT_COMP, without FEAT_DIAG) one grid for the whole
 //              pass from the mass bound `grid_mass` instead of a grid per
 //              thread and stage (no re-gridding between stages)
+//   FEAT_TMA   (FP32 y/z columns of a 3D field, with FEAT_NONE or FEAT_NL)
+//              each tile arrives in shared memory by one tensor copy (TMA,
+//              `tmap`), issued while the previous tile is transformed
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
-       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128, FEAT_COMP = 256, FEAT_GRIDM = 512 };
+       FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128, FEAT_COMP = 256, FEAT_GRIDM = 512, FEAT_TMA = 1024 };
+
+// Polls of a tile copy's mbarrier before a FEAT_TMA pass gives up (each
+// try_wait may suspend the thread for a while; a copy takes microseconds)
+constexpr uint32_t kTmaWaitPolls = 1u << 22;
 
 // A renormalisation factor as written by the last CTA of a pass: FP64 for the
 // FP64 kernels and a float copy for the FP32 ones (which then need no FP64
@@ -188,6 +196,11 @@ template <typename T> struct PassArgs {
     // stages of all lines, and one quantum for the whole pass replaces the
     // per-thread, per-stage ones (no re-gridding between stages)
     const double *grid_mass;
+    // FEAT_TMA: a CUtensorMap (global memory, 64-byte aligned) of the 3D
+    // field `in` with boxes of W x-adjacent columns by the whole line; the
+    // line axis (1: y, 2: z) and nx, which W divides
+    const void *tmap;
+    int taxis, tnx;
     // pipelined pass: 0 waits up to the default number of polls for a tile;
     // v > 0 waits v - 1 polls (host-side fault injection of a timeout)
     unsigned wait_polls;
@@ -308,10 +321,14 @@ template <typename T, int N, bool XL, int FEAT = 0> struct PassShape {
     static constexpr int DATA1 = (N2 == 1) ? 0 : (XL ? W * LS : W * N);
     // compensated passes keep the lo parts in a second array of the same layout
     static constexpr int DATA = DATA1 * ((FEAT & FEAT_COMP) ? 2 : 1);
+    // FEAT_TMA: the tile's staging buffer (first, 128-byte aligned) and the
+    // copy's mbarrier (after the tables)
+    static constexpr bool TMA = (FEAT & FEAT_TMA) != 0 && !XL;
+    static constexpr int STAGE = TMA ? W * N : 0;
     // w_n^{r k1} at k1*N2 + r (stage A) and at r*N1 + k1 (stage B) are the same
     // table when N1 == N2: then only one is held
     static constexpr bool TWB = N1 != N2;
-    static constexpr int SMEM_SLOTS = DATA + (TWB ? 6 : 4) * N;  // + twiddles + phase, hi and lo
+    static constexpr int SMEM_SLOTS = STAGE + DATA + (TWB ? 6 : 4) * N + (TMA ? 2 : 0);  // + tables hi and lo
     static constexpr size_t SMEM_BYTES = sizeof(vec2<T>) * SMEM_SLOTS;
 };
 
@@ -420,6 +437,9 @@ pass_kernel(const PassArgs<T> a)
     constexpr bool kAcc = kDiag || (FEAT & FEAT_ACC) != 0;
     constexpr bool kComp = (FEAT & FEAT_COMP) != 0 && sizeof(T) == 4;
     static_assert(!kComp || (MODE == MODE_FUSED && !kMask && !kPlane && !kImagM), "compensated: fused kinetic passes");
+    constexpr bool kTma = PassShape<T, N, XL, FEAT>::TMA;
+    static_assert(!kTma || (MODE == MODE_FUSED && !kComp && !kDiag && !kPlane && !kImagM && !kMask && !kAdj),
+                  "tensor-copy tiles: plain kinetic (+NL) passes");
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -428,14 +448,24 @@ pass_kernel(const PassArgs<T> a)
     constexpr int THREADS = S::THREADS;
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    V *sdata = reinterpret_cast<V *>(smem_raw);
+    V *stage = reinterpret_cast<V *>(smem_raw);  // FEAT_TMA staging tile (position-major, W per row)
+    (void)stage;
+    V *sdata = stage + S::STAGE;
     V *slo = sdata + S::DATA1;  // lo parts (FEAT_COMP)
     (void)slo;
     DWord<V> *stw = reinterpret_cast<DWord<V> *>(sdata + S::DATA);  // stage A [N], stage B [N]
     DWord<V> *stwB = S::TWB ? stw + N : stw;
     DWord<V> *sph = stw + (S::TWB ? 2 : 1) * N;                      // phase [N]
+    uint64_t *tbar = reinterpret_cast<uint64_t *>(sph + N);           // FEAT_TMA copy barrier
+    (void)tbar;
 
     const int tid = threadIdx.x;
+    if constexpr (kTma) {
+        if (tid == 0) {
+            mbar_init(tbar, 1u);
+            fence_mbar_init();
+        }
+    }
     // tables into shared memory, hi/lo halves packed per entry
     for (int i = tid; i < N; i += THREADS) {
         stw[i] = DWord<V>{a.tw[i], a.tw[N + i]};
@@ -495,6 +525,24 @@ pass_kernel(const PassArgs<T> a)
         else __syncthreads();
     };
     __syncthreads();  // tables ready
+    // FEAT_TMA: tile t is the box of W x-adjacent columns at (x0, rest); the
+    // first tile's copy starts now, each next one after the stage-A barrier
+    // of the current tile (when every thread has read the staging buffer)
+    uint32_t tphase = 0;
+    bool tdead = false;
+    auto tma_issue = [&](int t) {
+        const int g0 = t * W, x0 = g0 % a.tnx, rest = g0 / a.tnx;
+        mbar_arrive_expect_tx(tbar, (uint32_t)(S::STAGE * sizeof(V)));
+        if (a.taxis == 1) tma_load_3d(stage, a.tmap, x0, 0, rest, tbar);
+        else tma_load_3d(stage, a.tmap, x0, rest, 0, tbar);
+    };
+    (void)tma_issue;
+    if constexpr (kTma) {
+        if (tid == 0 && (int)blockIdx.x < ntiles) {
+            asm volatile("fence.proxy.async.global;" ::: "memory");  // the previous grid's field writes
+            tma_issue(blockIdx.x);
+        }
+    }
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int g = tile * W + w;
     const bool valid = g < a.nlines;
@@ -513,9 +561,18 @@ pass_kernel(const PassArgs<T> a)
 
     V v[N1];
     if constexpr (MODE != MODE_INV) {
+        if constexpr (kTma) {
+            // the tile's copy: a bounded wait (a copy that never lands is
+            // reported, not waited on forever), then the thread's values
+            tdead = tdead || !mbar_wait_bounded(tbar, tphase, kTmaWaitPolls);
+            tphase ^= 1u;
 #pragma unroll
-        for (int j = 0; j < N1; j++) {
-            v[j] = a.in[base + (uint32_t)(r + N2 * j) * st];  // invalid threads read line 0 ...
+            for (int j = 0; j < N1; j++) v[j] = stage[(r + N2 * j) * W + w];
+        } else {
+#pragma unroll
+            for (int j = 0; j < N1; j++) {
+                v[j] = a.in[base + (uint32_t)(r + N2 * j) * st];  // invalid threads read line 0 ...
+            }
         }
         if constexpr (MODE == MODE_FUSED || MODE == MODE_DIAG) {
             if (!valid) {  // ... and sum nothing
@@ -744,7 +801,22 @@ pass_kernel(const PassArgs<T> a)
                 }
                 sdata[sidx(m)] = t;
             }
-            line_sync();
+            if constexpr (kTma) {
+                // every thread has read the staging buffer: the next tile's
+                // copy may land in it.  A copy that timed out stops the CTA
+                // here (the status word reports it; the CTA still joins the
+                // reduction below so the grid's arrival count stays whole).
+                if (__syncthreads_or(tdead)) {
+                    if (tid == 0) {
+                        mbar_wait_bounded(tbar, tphase ^ 1u, kTmaWaitPolls);  // its own copy, if it lands late
+                        if (a.fin_status) atomicOr(a.fin_status, 2);
+                    }
+                    break;
+                }
+                if (tid == 0 && tile + (int)gridDim.x < ntiles) tma_issue(tile + (int)gridDim.x);
+            } else {
+                line_sync();
+            }
         }
         // ---- stage B: items k1 = r + P*i
         constexpr int NI = N1 / N2;

@@ -1,4 +1,4 @@
-"""Generates tests/golden/cfg2_3d_128_ground.npz: the cfg2 imaginary-time
+"""Generates tests/golden/cfg2_3d_128.ground.npz: the cfg2 imaginary-time
 ground state at its full size (128^3 on [-10, 10]^3, V = (x^2 + y^2 + 4 z^2)/2,
 g = 2000, dt = 1e-3) run by the FP64 oracle (oracle/gp_oracle.c) until
 |mu_n - mu_{n-10}| < 1e-10 with mu evaluated every 10 steps -- the stopping
@@ -50,7 +50,7 @@ def main():
                sample=np.ascontiguousarray(psi[::8, ::8, ::8]),
                line_x=psi[:, mid[1], mid[2]].copy(), line_y=psi[mid[0], :, mid[2]].copy(),
                line_z=psi[mid[0], mid[1], :].copy(), max_abs=np.max(np.abs(psi)))
-    path = sys.argv[1] if len(sys.argv) > 1 else os.path.join(HERE, "cfg2_3d_128_ground.npz")
+    path = sys.argv[1] if len(sys.argv) > 1 else os.path.join(HERE, "cfg2_3d_128.ground.npz")
     np.savez_compressed(path, **out)
     print("steps", done, "mu", e[4], "seconds", time.time() - t0)
 

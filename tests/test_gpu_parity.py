@@ -355,7 +355,7 @@ def test_cfg2_ground_state_small(sfd, O, W):
 def test_cfg2_fullsize_ground_state(sfd, O, W):
     """cfg2 at its full size (128^3, g = 2000, anisotropic trap, dt = 1e-3)
     run to the ground state, against the FP64 oracle's run
-    (tests/golden/cfg2_3d_128_ground.npz, made by make_cfg2_ground.py: 16410
+    (tests/golden/cfg2_3d_128.ground.npz, made by make_cfg2_ground.py: 16410
     steps to |mu_n - mu_{n-10}| < 1e-10).
     * FP64 gpss_ground_state stops at the oracle's step -- or one check later:
       the oracle's last difference is 9.98e-11, within rounding of the
@@ -363,9 +363,13 @@ def test_cfg2_fullsize_ground_state(sfd, O, W):
     * FP64, the oracle's step count: the five energies within 1e-11 and the
       field within 1e-10 (of its largest value) of the oracle's;
     * FP32 stages with FP64 reductions and renormalisation, the same steps:
-      mu within 1e-6, the field within 1e-5."""
+      mu within 1e-6, the field within 2e-4 of its largest value.  Near the
+      ground state each step damps the slowest excitation only by about
+      gap * dt ~ 1e-3, so the FP32 rounding of every step accumulates there
+      about 1/(gap dt) ~ 1e3 times (measured: 5.3e-5); mu is variational
+      (second order in that error)."""
     import os
-    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "cfg2_3d_128_ground.npz"))
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "cfg2_3d_128.ground.npz"))
     c = W.cfg2(128)
     nref, eref = int(z["nsteps"]), z["energies"]
     mid = [n // 2 for n in c["shape"]]
@@ -402,7 +406,7 @@ def test_cfg2_fullsize_ground_state(sfd, O, W):
     close(got64, 1e-10)
     e32, got32 = out["fp32"]
     assert abs(e32[4] - eref[4]) <= 1e-6 * abs(eref[4])
-    close(got32, 1e-5)
+    close(got32, 2e-4)
     print(f"cfg2 128^3 ground state: {steps} steps (oracle {nref}), mu FP64 {mu:.12f} "
           f"(oracle {eref[4]:.12f}), FP32 {e32[4]:.10f}")
 
@@ -429,7 +433,7 @@ def _golden():
     import os
     here = os.path.join(os.path.dirname(__file__), "golden")
     return sorted(os.path.join(here, f) for f in os.listdir(here)
-                  if f.endswith(".npz") and not f.endswith((".grad.npz", ".solver.npz")))
+                  if f.endswith(".npz") and not f.endswith((".grad.npz", ".solver.npz", ".ground.npz")))
 
 
 @pytest.mark.parametrize("path", _golden(), ids=lambda p: p.split("/")[-1][:-4])

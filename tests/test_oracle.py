@@ -178,7 +178,7 @@ def test_golden_fixtures_reproduce(O):
     """The committed golden vectors (tests/golden/) are what the oracle computes."""
     import os
     here = os.path.join(os.path.dirname(__file__), "golden")
-    names = sorted(f for f in os.listdir(here) if f.endswith(".npz") and not f.endswith((".grad.npz", ".solver.npz")))
+    names = sorted(f for f in os.listdir(here) if f.endswith(".npz") and not f.endswith((".grad.npz", ".solver.npz", ".ground.npz")))
     assert names, "no golden fixtures"
     for nm in names:
         z = np.load(os.path.join(here, nm))
