@@ -82,6 +82,27 @@ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c)
     return upk(d);
 }
 __device__ __forceinline__ float2 p_neg(float2 a) { return make_float2(-a.x, -a.y); }
+// (x, y) -> (y, x): register renaming or moves, no arithmetic
+__device__ __forceinline__ float2 p_swap(float2 a) { return make_float2(a.y, a.x); }
+// -x by a flip of the sign bit on the integer ALU.  GB300 runs packed f32x2
+// and scalar FP32 instructions on the same FMA pipes, and a stream that mixes
+// them issues at ~75 % of the rate of either kind alone (measured), so the
+// compensated code keeps scalar FP32 instructions out: a sign that differs
+// between the two lanes is either a packed multiply-add by a +-1 pair or,
+// for run-time table constants, this integer xor (which co-issues).
+__device__ __forceinline__ float negx(float a)
+{
+    unsigned u = __float_as_uint(a);
+    asm("xor.b32 %0, %0, 0x80000000;" : "+r"(u));
+    return __uint_as_float(u);
+}
+// a + DIR * i * b (S = (-DIR, DIR)) or a - DIR * i * b (S = (DIR, -DIR)) as
+// one packed fma of the lane-swapped b by the sign pair: exact products by
+// +-1, one rounding of the sum (exact for two values on one grid)
+template <int SX, int SY> __device__ __forceinline__ float2 p_addrot(float2 a, float2 b)
+{
+    return p_fma(p_swap(b), make_float2((float)SX, (float)SY), a);
+}
 
 // ---------------------------------------------------------------- the grid --
 // C = 1.5 * 2^23 * q (both lanes) for the quantum q = 2^(E - 17), E the
@@ -140,11 +161,21 @@ __device__ __forceinline__ float2 c_round(const cdf &a) { return p_add(a.h, a.l)
 __device__ __forceinline__ cdf g_add(const cdf &a, const cdf &b) { return cdf{p_add(a.h, b.h), p_add(a.l, b.l)}; }
 __device__ __forceinline__ cdf g_sub(const cdf &a, const cdf &b) { return cdf{p_sub(a.h, b.h), p_sub(a.l, b.l)}; }
 
-// multiply by DIR*i (exact)
+// multiply by DIR*i (exact): (x, y) -> (-DIR y, DIR x), one packed multiply
+// of the swapped lanes by a sign pair per part
 template <int DIR> __device__ __forceinline__ cdf g_muli(const cdf &a)
 {
-    if (DIR < 0) return cdf{make_float2(a.h.y, -a.h.x), make_float2(a.l.y, -a.l.x)};
-    return cdf{make_float2(-a.h.y, a.h.x), make_float2(-a.l.y, a.l.x)};
+    const float2 S = make_float2((float)-DIR, (float)DIR);
+    return cdf{p_mul(p_swap(a.h), S), p_mul(p_swap(a.l), S)};
+}
+// a + DIR*i*b and a - DIR*i*b (exact on the grid)
+template <int DIR> __device__ __forceinline__ cdf g_addi(const cdf &a, const cdf &b)
+{
+    return cdf{p_addrot<-DIR, DIR>(a.h, b.h), p_addrot<-DIR, DIR>(a.l, b.l)};
+}
+template <int DIR> __device__ __forceinline__ cdf g_subi(const cdf &a, const cdf &b)
+{
+    return cdf{p_addrot<DIR, -DIR>(a.h, b.h), p_addrot<DIR, -DIR>(a.l, b.l)};
 }
 __device__ __forceinline__ cdf g_neg(const cdf &a) { return cdf{p_neg(a.h), p_neg(a.l)}; }
 
@@ -159,11 +190,11 @@ __device__ __forceinline__ cdf g_rmul2(const cdf &a, float hi, float lo, float2 
 
 // a * (bh + bl), b a double-word complex constant, as packed pairs:
 //   (re, im) = (ax, ax) * (bx, by) + (ay, ay) * (-by, bx)
-// each of the two packed products is gridded with its exact residual
-__device__ __forceinline__ cdf g_cmul2(const cdf &a, float2 bh, float2 bl, float2 C)
+// each of the two packed products is gridded with its exact residual;
+// b2, bl2 are the rotated pairs (-by, bx) of bh, bl
+__device__ __forceinline__ cdf g_cmul2r(const cdf &a, float2 bh, float2 b2, float2 bl, float2 bl2, float2 C)
 {
     const float2 X = make_float2(a.h.x, a.h.x), Y = make_float2(a.h.y, a.h.y);
-    const float2 b2 = make_float2(-bh.y, bh.x), bl2 = make_float2(-bl.y, bl.x);
     const float2 u = p_sub(p_fma(X, bh, C), C);
     const float2 v = p_sub(p_fma(Y, b2, C), C);
     // the low parts in two independent chains (2% faster at 256^3 than one
@@ -174,10 +205,32 @@ __device__ __forceinline__ cdf g_cmul2(const cdf &a, float2 bh, float2 bl, float
     l2 = p_fma(make_float2(a.l.y, a.l.y), b2, l2);
     return cdf{p_add(u, v), p_add(l1, l2)};
 }
-// a * conj(bh + bl)
+// a * (bh + bl) for a run-time constant (a table entry): the one-lane signs
+// of the rotated pairs on the integer ALU
+__device__ __forceinline__ cdf g_cmul2(const cdf &a, float2 bh, float2 bl, float2 C)
+{
+    return g_cmul2r(a, bh, make_float2(negx(bh.y), bh.x), bl, make_float2(negx(bl.y), bl.x), C);
+}
+// a * conj(bh + bl) for a run-time constant: conj(b) = (bx, -by), rotated (by, bx)
 __device__ __forceinline__ cdf g_cmulc2(const cdf &a, float2 bh, float2 bl, float2 C)
 {
-    return g_cmul2(a, make_float2(bh.x, -bh.y), make_float2(bl.x, -bl.y), C);
+    return g_cmul2r(a, make_float2(bh.x, negx(bh.y)), p_swap(bh), make_float2(bl.x, negx(bl.y)), p_swap(bl), C);
+}
+// a * (bh + bl) for a compile-time constant: (re, im) = a (c, c) + swap(a) (-s, s)
+// -- the constant pairs are immediates, so the data needs one lane swap per
+// part instead of two lane broadcasts
+__device__ __forceinline__ cdf g_cmul2k(const cdf &a, float2 bh, float2 bl, float2 C)
+{
+    const float2 c = make_float2(bh.x, bh.x), s = make_float2(-bh.y, bh.y);
+    const float2 cl = make_float2(bl.x, bl.x), sl = make_float2(-bl.y, bl.y);
+    const float2 sh = p_swap(a.h);
+    const float2 u = p_sub(p_fma(a.h, c, C), C);
+    const float2 v = p_sub(p_fma(sh, s, C), C);
+    float2 l1 = p_fma(a.h, cl, p_fma(a.h, c, p_neg(u)));
+    float2 l2 = p_fma(sh, sl, p_fma(sh, s, p_neg(v)));
+    l1 = p_fma(a.l, c, l1);
+    l2 = p_fma(p_swap(a.l), s, l2);
+    return cdf{p_add(u, v), p_add(l1, l2)};
 }
 
 // multiply by w16^m = exp(DIR * 2 pi i m / 16) for a compile-time m
@@ -190,15 +243,15 @@ template <int M, int DIR> __device__ __forceinline__ cdf g_mulw16(const cdf &a, 
     else if constexpr (m == 8) return g_neg(a);
     else if constexpr (m == 12) return g_muli<-DIR>(a);
     else if constexpr (m % 2 == 0) {
-        // odd multiple of pi/4: value = (sc + i ss) / sqrt2 with sc, ss = +-1
+        // odd multiple of pi/4: value = (sc + i ss) / sqrt2 with sc, ss = +-1.
+        // a (sc + i ss) = sc (a + i (ss/sc) a): one exact packed fma of the
+        // swapped lanes by a sign pair, then the product by sc sqrt(1/2)
         constexpr int q = m / 2;
-        constexpr float sc = (q == 1 || q == 7) ? 1.f : -1.f;
-        constexpr float ss = ((q == 1 || q == 3) ? 1.f : -1.f) * (float)DIR;
-        // (sc ax - ss ay, ss ax + sc ay) = (sc, ss) ax + (-ss, sc) ay: exact
-        // sign changes and one exact grid add, then the sqrt(1/2) product
-        const cdf A{make_float2(sc * a.h.x, ss * a.h.x), make_float2(sc * a.l.x, ss * a.l.x)};
-        const cdf B{make_float2(-ss * a.h.y, sc * a.h.y), make_float2(-ss * a.l.y, sc * a.l.y)};
-        return g_rmul2(g_add(A, B), K::Hh, K::Hl, C);
+        constexpr int sc = (q == 1 || q == 7) ? 1 : -1;
+        constexpr int ss = ((q == 1 || q == 3) ? 1 : -1) * DIR;
+        constexpr int r = ss * sc;  // a + i r a = (x - r y, y + r x)
+        const cdf t{p_addrot<-r, r>(a.h, a.h), p_addrot<-r, r>(a.l, a.l)};
+        return g_rmul2(t, (float)sc * K::Hh, (float)sc * K::Hl, C);
     } else {
         constexpr int ci = (m == 1 || m == 15) ? 1 : (m == 3 || m == 13) ? 2 : (m == 5 || m == 11) ? -2 : -1;
         constexpr int si = (m == 1 || m == 7) ? 2 : (m == 3 || m == 5) ? 1 : (m == 9 || m == 15) ? -2 : -1;
@@ -206,7 +259,7 @@ template <int M, int DIR> __device__ __forceinline__ cdf g_mulw16(const cdf &a, 
         const float crl = (ci == 1 || ci == -1) ? (ci > 0 ? K::C1l : -K::C1l) : (ci > 0 ? K::S1l : -K::S1l);
         const float srh = (si == 2 || si == -2) ? (si > 0 ? K::S1h : -K::S1h) : (si > 0 ? K::C1h : -K::C1h);
         const float srl = (si == 2 || si == -2) ? (si > 0 ? K::S1l : -K::S1l) : (si > 0 ? K::C1l : -K::C1l);
-        return g_cmul2(a, make_float2(crh, (float)DIR * srh), make_float2(crl, (float)DIR * srl), C);
+        return g_cmul2k(a, make_float2(crh, (float)DIR * srh), make_float2(crl, (float)DIR * srl), C);
     }
 }
 
@@ -220,11 +273,22 @@ template <int DIR> __device__ __forceinline__ void g_dft2(cdf &a0, cdf &a1)
 template <int DIR> __device__ __forceinline__ void g_dft4(cdf &a0, cdf &a1, cdf &a2, cdf &a3)
 {
     const cdf s02 = g_add(a0, a2), d02 = g_sub(a0, a2);
-    const cdf s13 = g_add(a1, a3), t = g_muli<DIR>(g_sub(a1, a3));
+    const cdf s13 = g_add(a1, a3), d13 = g_sub(a1, a3);
     a0 = g_add(s02, s13);
     a2 = g_sub(s02, s13);
-    a1 = g_add(d02, t);
-    a3 = g_sub(d02, t);
+    a1 = g_addi<DIR>(d02, d13);
+    a3 = g_subi<DIR>(d02, d13);
+}
+// the same with a2 still to be multiplied by DIR*i (the twiddle w16^4 of the
+// 16-point tail, folded into the butterfly)
+template <int DIR> __device__ __forceinline__ void g_dft4_i2(cdf &a0, cdf &a1, cdf &a2, cdf &a3)
+{
+    const cdf s02 = g_addi<DIR>(a0, a2), d02 = g_subi<DIR>(a0, a2);
+    const cdf s13 = g_add(a1, a3), d13 = g_sub(a1, a3);
+    a0 = g_add(s02, s13);
+    a2 = g_sub(s02, s13);
+    a1 = g_addi<DIR>(d02, d13);
+    a3 = g_subi<DIR>(d02, d13);
 }
 
 // the 16-point transform after its first radix-4 level: b[j1 + 4 k1] holds
@@ -235,7 +299,6 @@ template <int DIR> __device__ __forceinline__ void g_dft16_tail(cdf *a, float2 C
     a[9] = g_mulw16<2, DIR>(a[9], C);
     a[13] = g_mulw16<3, DIR>(a[13], C);
     a[6] = g_mulw16<2, DIR>(a[6], C);
-    a[10] = g_mulw16<4, DIR>(a[10], C);
     a[14] = g_mulw16<6, DIR>(a[14], C);
     a[7] = g_mulw16<3, DIR>(a[7], C);
     a[11] = g_mulw16<6, DIR>(a[11], C);
@@ -244,7 +307,8 @@ template <int DIR> __device__ __forceinline__ void g_dft16_tail(cdf *a, float2 C
 #pragma unroll
     for (int k1 = 0; k1 < 4; k1++) {
         cdf u0 = a[4 * k1 + 0], u1 = a[4 * k1 + 1], u2 = a[4 * k1 + 2], u3 = a[4 * k1 + 3];
-        g_dft4<DIR>(u0, u1, u2, u3);
+        if (k1 == 2) g_dft4_i2<DIR>(u0, u1, u2, u3);  // a[10] carries w16^4 = DIR*i
+        else g_dft4<DIR>(u0, u1, u2, u3);
         o[k1] = u0;
         o[k1 + 4] = u1;
         o[k1 + 8] = u2;
@@ -257,15 +321,18 @@ template <int DIR> __device__ __forceinline__ void g_dft16_tail(cdf *a, float2 C
 template <int DIR> __device__ __forceinline__ void g_dft8_tail(cdf *a, float2 C)
 {
     a[3] = g_mulw16<2, DIR>(a[3], C);
-    a[5] = g_mulw16<4, DIR>(a[5], C);
     a[7] = g_mulw16<6, DIR>(a[7], C);
     cdf o[8];
 #pragma unroll
     for (int k1 = 0; k1 < 4; k1++) {
-        cdf u0 = a[2 * k1], u1 = a[2 * k1 + 1];
-        g_dft2<DIR>(u0, u1);
-        o[k1] = u0;
-        o[k1 + 4] = u1;
+        const cdf u0 = a[2 * k1], u1 = a[2 * k1 + 1];
+        if (k1 == 2) {  // a[5] carries w16^4 = DIR*i
+            o[k1] = g_addi<DIR>(u0, u1);
+            o[k1 + 4] = g_subi<DIR>(u0, u1);
+        } else {
+            o[k1] = g_add(u0, u1);
+            o[k1 + 4] = g_sub(u0, u1);
+        }
     }
 #pragma unroll
     for (int i = 0; i < 8; i++) a[i] = o[i];
