@@ -380,8 +380,9 @@ def measure_adjoint(sfd, W):
     c = W.cfg4(256)
     out = {"workload": "cfg4: 2D adjoint, 256^2 on [-8,8]^2, trap + learnable V, g=500, dt=1e-3, "
                        "2000 steps, K=50, loss 1-|<psi_t|psi(T)>|^2"}
-    for prec in ("fp32", "fp64"):
-        f, m = _model(sfd, c, prec, V=c["V"])
+    grads = {}
+    for tag, prec, comp in (("fp32", "fp32", False), ("fp32_compensated", "fp32", True), ("fp64", "fp64", False)):
+        f, m = _model(sfd, c, prec, V=c["V"], compensated=comp)
         m.adjoint(c["target"], 100, 50)  # warm-up
         t = []
         for _ in range(3):
@@ -389,8 +390,12 @@ def measure_adjoint(sfd, W):
             loss, dv, g0 = m.adjoint(c["target"], c["nsteps"], c["K"])
             t.append(time.perf_counter() - t0)
         m.close(download=False)
-        out[prec] = {"s_per_gradient": min(t), "loss": loss,
-                     "forward_plus_backward_cell_steps_per_s": 256 * 256 * c["nsteps"] / min(t)}
+        grads[tag] = dv
+        out[tag] = {"s_per_gradient": min(t), "loss": loss,
+                    "forward_plus_backward_cell_steps_per_s": 256 * 256 * c["nsteps"] / min(t)}
+    for tag in ("fp32", "fp32_compensated"):
+        out[tag]["dLdV_rel_l2_vs_fp64"] = float(np.linalg.norm(grads[tag] - grads["fp64"]) /
+                                                np.linalg.norm(grads["fp64"]))
     return out
 
 

@@ -46,6 +46,10 @@ static int adj_group(gpss_ctx *c, void *buf, double dtl, bool reverse, bool nl, 
         const void *ph;
         GPSS_TRY(get_phase(c, axis, dtl, 0, 1, &ph, &a.prow));
         a.phase = (const vec2<T> *)ph;
+        // a compensated FP32 context differentiates with compensated passes
+        // (forward, recompute and backward alike, so the recomputed states
+        // stay bitwise those of the forward)
+        a.comp = sizeof(T) == 4 && (c->flags & GPSS_FLAG_COMPENSATED) != 0;
         if (step == c->ndim - 1 && (nl || adj_pre)) {
             a.V = c->have_V ? (const T *)c->V : nullptr;
             a.nl_beta = c->beta;

@@ -78,12 +78,17 @@ cudaError_t launch_comp_f32(bool xl, int n, const PassArgs<float> &a, int blocks
 template <int N, bool XL>
 static cudaError_t launch_comp_mode(const PassArgs<float> &a, int blocks, cudaStream_t s)
 {
-    // the split-step kinetic passes only: phase, prescale, NL epilogue, sums
-    if (a.mask_lim || a.acc || a.pre_out || a.adj_pre || a.nl_pre || a.dot_with || a.plane_nl ||
-        a.plane_scale || !a.phase)
+    // the split-step kinetic passes only: phase, prescale, NL epilogue, sums,
+    // and the discrete adjoint's epilogues (pre_out, adj_pre)
+    if (a.mask_lim || a.acc || a.nl_pre || a.dot_with || a.plane_nl || a.plane_scale || !a.phase)
         return cudaErrorInvalidValue;
     const bool diag = (a.red & (RED_POINT | RED_KIN)) || a.prow != 0;
     const bool nl = a.nl_mode != NL_NONE || (a.red & RED_MASS);
+    if (a.pre_out || a.adj_pre) {  // per-thread grids: the adjoint runs without the mass lock
+        if (diag || a.grid_mass || a.red) return cudaErrorInvalidValue;
+        if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_ADJ | FEAT_NL>(a, blocks, s);
+        return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_ADJ>(a, blocks, s);
+    }
     if (diag) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_ALL>(a, blocks, s);
     if (a.grid_mass) {  // one grid per pass from the mass bound
         if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_GRIDM | FEAT_NL>(a, blocks, s);
