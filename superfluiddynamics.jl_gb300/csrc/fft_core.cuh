@@ -56,6 +56,29 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b)
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pack_f2(a)), "l"(pack_f2(b)));
     return unpack_f2(d);
 }
+// a * b + c and a * b lane by lane (one rounding each, as the scalar fma and mul)
+__device__ __forceinline__ float2 pfma_f2(float2 a, float2 b, float2 c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pack_f2(a)), "l"(pack_f2(b)), "l"(pack_f2(c)));
+    return unpack_f2(d);
+}
+__device__ __forceinline__ float2 pmul_f2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pack_f2(a)), "l"(pack_f2(b)));
+    return unpack_f2(d);
+}
+__device__ __forceinline__ float2 swap_f2(float2 a) { return make_float2(a.y, a.x); }
+#endif
+// FP32 DFT-4 butterflies and the w16^2k twiddles in packed form: a sign that
+// differs between the lanes is a packed multiply-add of the lane-swapped
+// value by a +-1 pair (exact products), rounding exactly as the scalar
+// expressions it replaces (256^3 plain z pass 67.8 -> 67.1 us; the plain
+// passes are not bound by their FMA pipes, and packed double-word constant
+// products measured no faster than the scalar ones kept below)
+#ifndef GPSS_PACKED_DFT
+#define GPSS_PACKED_DFT GPSS_PACKED_F32
 #endif
 // a * b
 template <typename V> __device__ __forceinline__ V cmul(V a, V b)
@@ -118,19 +141,32 @@ template <int M, int DIR, typename V> __device__ __forceinline__ V mul_w16(V a)
     using T = decltype(V::x);
     using K = DftConst<T>;
     constexpr int m = ((M % 16) + 16) % 16;
+    constexpr bool packed = GPSS_PACKED_DFT && sizeof(T) == 4;
     if constexpr (m == 0) return a;
+    else if constexpr (m == 4 && packed) return pmul_f2(swap_f2(a), make_float2((float)-DIR, (float)DIR));
     else if constexpr (m == 4) return mul_i<DIR>(a);
     else if constexpr (m == 8) return mk<V>(-a.x, -a.y);
+    else if constexpr (m == 12 && packed) return pmul_f2(swap_f2(a), make_float2((float)DIR, (float)-DIR));
     else if constexpr (m == 12) return mul_i<-DIR>(a);
     else if constexpr (m % 2 == 0) {
         // odd multiple of pi/4: value = (sc + i ss) / sqrt2 with sc, ss = +-1
         constexpr int q = m / 2;  // 1, 3, 5, 7
         constexpr int sc = (q == 1 || q == 7) ? 1 : -1;
         constexpr int ss = ((q == 1 || q == 3) ? 1 : -1) * DIR;
-        // (a.x + i a.y)(sc + i ss) = (sc a.x - ss a.y) + i (ss a.x + sc a.y)
-        const T re = sc * a.x - ss * a.y;
-        const T im = ss * a.x + sc * a.y;
-        return mk<V>(rmul2(re, K::Hh, K::Hl), rmul2(im, K::Hh, K::Hl));
+        if constexpr (packed) {
+            // (sc x - ss y, ss x + sc y) = sc (x - r y, y + r x), r = ss sc: one
+            // exact packed fma of the swapped lanes by a sign pair, the sign sc
+            // folded into sqrt(1/2)
+            constexpr int r = ss * sc;
+            const float2 t = pfma_f2(swap_f2(a), make_float2((float)-r, (float)r), a);
+            const float hh = (float)sc * K::Hh, hl = (float)sc * K::Hl;
+            return pfma_f2(t, make_float2(hh, hh), pmul_f2(t, make_float2(hl, hl)));
+        } else {
+            // (a.x + i a.y)(sc + i ss) = (sc a.x - ss a.y) + i (ss a.x + sc a.y)
+            const T re = sc * a.x - ss * a.y;
+            const T im = ss * a.x + sc * a.y;
+            return mk<V>(rmul2(re, K::Hh, K::Hl), rmul2(im, K::Hh, K::Hl));
+        }
     } else {
         // odd multiple of pi/8: cos/sin are +-C1 / +-S1
         constexpr int ci = (m == 1 || m == 15) ? 1 : (m == 3 || m == 13) ? 2 : (m == 5 || m == 11) ? -2 : -1;
@@ -157,9 +193,13 @@ template <int DIR, typename V> __device__ __forceinline__ void dft4(V &a0, V &a1
     V s13 = cadd(a1, a3), t = csub(a1, a3);
     a0 = cadd(s02, s13);
     a2 = csub(s02, s13);
-    // a1 = d02 + DIR i t, a3 = d02 - DIR i t, written per component (the
-    // swap of re/im is free here, but not inside a packed FP32 operation)
-    if (DIR < 0) {
+    // a1 = d02 + DIR i t, a3 = d02 - DIR i t: per component, or (FP32) one
+    // packed fma each of the lane-swapped t by a sign pair
+    if constexpr (GPSS_PACKED_DFT && sizeof(decltype(V::x)) == 4) {
+        const float2 ts = make_float2(t.y, t.x);
+        a1 = pfma_f2(ts, make_float2((float)-DIR, (float)DIR), d02);
+        a3 = pfma_f2(ts, make_float2((float)DIR, (float)-DIR), d02);
+    } else if (DIR < 0) {
         a1 = mk<V>(d02.x + t.y, d02.y - t.x);
         a3 = mk<V>(d02.x - t.y, d02.y + t.x);
     } else {
