@@ -17,6 +17,12 @@ from helpers import random_field, run_model
 
 pytestmark = pytest.mark.gpu
 
+# full-size properties of the compensated passes (measured on GB300: linear
+# flow 2.0e-7 against 1.0e-6 for the plain passes, time reversal 5.5e-7
+# against 2.3e-6)
+LINEAR_FLOW_BAR_COMP = 5e-7
+REVERSAL_BAR_COMP = 1.5e-6
+
 TOL64 = 1e-12
 TOL32 = 1e-5
 
@@ -556,13 +562,15 @@ def test_fp32_compensated_imaginary_unmerged(sfd, O, shape):
 
 
 # ------------------------------------------- full-size (256^3) properties --
-def test_fullsize_linear_flow_is_exact_fp32(sfd, O, W):
+@pytest.mark.parametrize("compensated,bar", [(False, 3e-6), (True, LINEAR_FLOW_BAR_COMP)])
+def test_fullsize_linear_flow_is_exact_fp32(sfd, O, W, compensated, bar):
     """beta = V = 0 at 256^3: every merged FP32 pass applies the exact kinetic
     factor, so 20 steps equal exp(i coeffD |k|^2 t) on the spectrum (numpy
-    FFT in complex128 of the same input) to FP32 round-off."""
+    FFT in complex128 of the same input) to FP32 round-off.  The compensated
+    passes leave only the rounding of each pass's store (63 of them here)."""
     c = W.cfg1(256)
     got = run_model(sfd, c["shape"], c["bounds"], c["psi"], coeffD=c["coeffD"], beta=0.0, dt=c["dt"],
-                    nsteps=20, precision="fp32")
+                    nsteps=20, precision="fp32", compensated=compensated)
     F = np.fft.fftn(c["psi"])
     k2 = 0
     for a in range(3):
@@ -571,10 +579,13 @@ def test_fullsize_linear_flow_is_exact_fp32(sfd, O, W):
         s[a] = 256
         k2 = k2 + xi.reshape(s) ** 2
     want = np.fft.ifftn(F * np.exp(1j * c["coeffD"] * k2 * (20 * c["dt"])))
-    assert O.rel_l2(got, want) < 3e-6
+    err = O.rel_l2(got, want)
+    print(f"linear flow, compensated={compensated}: rel-L2 {err:.3e}")
+    assert err < bar
 
 
-def test_fullsize_time_reversal_fp32(sfd, O, W):
+@pytest.mark.parametrize("compensated,bar", [(False, 1e-5), (True, REVERSAL_BAR_COMP)])
+def test_fullsize_time_reversal_fp32(sfd, O, W, compensated, bar):
     """Strang splitting is time-reversible: N(-dt) undoes N(dt) (it keeps
     |psi|), the kinetic flows are unitary.  40 steps forward then 40 with -dt
     at 256^3 in FP32 return the initial field to round-off, and the FP64
@@ -584,7 +595,7 @@ def test_fullsize_time_reversal_fp32(sfd, O, W):
     f = sfd.Field(g)
     f.phi = c["psi"]
     p = sfd.GrossPitaevskiiParameters(sfd.PotentialZero(f), coeffD=c["coeffD"], beta=c["beta"])
-    n = sfd.NumModelSplit2(f, p, c["dt"], 1, 1, precision="fp32")
+    n = sfd.NumModelSplit2(f, p, c["dt"], 1, 1, precision="fp32", compensated=compensated)
     e0 = n.energies()
     n.step(40)
     mid = f.phi.copy()
@@ -593,8 +604,10 @@ def test_fullsize_time_reversal_fp32(sfd, O, W):
     back = f.phi.copy()
     e1 = n.energies()
     n.close()
+    err = O.rel_l2(back, c["psi"])
+    print(f"time reversal, compensated={compensated}: rel-L2 {err:.3e}, energy {abs(e1[3] - e0[3]) / abs(e0[3]):.2e}")
     assert O.rel_l2(mid, c["psi"]) > 1e-2          # the field did move
-    assert O.rel_l2(back, c["psi"]) < 1e-5
+    assert err < bar
     assert abs(e1[3] - e0[3]) < 1e-5 * abs(e0[3])
 
 
