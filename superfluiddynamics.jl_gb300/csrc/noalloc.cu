@@ -191,7 +191,11 @@ extern "C" int gpss_energy_noalloc(int ndim, const int64_t *n, const double *lo,
         if (!(hi[a] > lo[a])) return noalloc_fail(GPSS_EINVAL, "need lo < hi on every axis");
         n3[a] = n[a];
     }
-    // the partial sums of the largest pass must fit the fixed scratch
+    // the partial sums of the largest pass must fit the fixed scratch, counted
+    // from the tile count (an upper bound on the grid, which may be capped at
+    // one wave).  The largest accepted field, 256^3 in FP64 (64-thread CTAs,
+    // 4 lines each: 16384 tiles x 5 sums x 8 B = 640 KiB), fits with a 1.6x
+    // margin, so today this refusal is a guard for changed launch shapes.
     const int64_t total = n3[0] * n3[1] * n3[2];
     for (int a = 0; a < ndim; a++) {
         const int W = precision == GPSS_FP32 ? pass_lines_per_cta_f32((int)n3[a], a == 0)
