@@ -169,12 +169,33 @@ cudaError_t im_dot2(const vec2<T> *a1, const vec2<T> *b1, const vec2<T> *a2, con
                     double *partials, double *out, cudaStream_t s);
 template <typename T>
 cudaError_t im_axmy(vec2<T> *out, const vec2<T> *x, double alpha, const vec2<T> *y, int64_t total, cudaStream_t s);
+
+// The scalars of one BiCGStab solve (krylov.jl:1-67), kept on the device so
+// that iterations run without a host round trip: the dot products are
+// finished on the device, one thread forms alpha, omega, beta and the
+// stopping test from them in FP64 (the same operations, in the same order, as
+// the reference), and the vector updates read them from here.  Once `done`
+// is set (converged, out of iterations, or a non-finite residual) every later
+// update of the same solve is a no-op, so the host may issue iterations in
+// chunks and read this back once per chunk.
+struct KrylovDev {
+    double normb, rr2, alpha, omega, beta;
+    int done, niter, nonfinite, it;
+};
+cudaError_t kry_init(KrylovDev *K, const double *dots, cudaStream_t s);
+cudaError_t kry_alpha(KrylovDev *K, const double *dots, cudaStream_t s);
+cudaError_t kry_omega(KrylovDev *K, const double *dots, cudaStream_t s);
+cudaError_t kry_check(KrylovDev *K, const double *dots, double tol, int nkrylov, cudaStream_t s);
+// s = r - alpha Ap;  phi = (phi + alpha p) + omega s, r = s - omega As;  p = r + beta (p - omega Ap)
 template <typename T>
-cudaError_t im_update(vec2<T> *phi, const vec2<T> *p, const vec2<T> *sv, const vec2<T> *As, vec2<T> *r, double alpha,
-                      double omega, int64_t total, cudaStream_t s);
+cudaError_t im_axmy_k(vec2<T> *out, const vec2<T> *x, const vec2<T> *y, const KrylovDev *K, int64_t total,
+                      cudaStream_t s);
 template <typename T>
-cudaError_t im_pdir(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, double beta, double omega, int64_t total,
-                    cudaStream_t s);
+cudaError_t im_update_k(vec2<T> *phi, const vec2<T> *p, const vec2<T> *sv, const vec2<T> *As, vec2<T> *r,
+                        const KrylovDev *K, int64_t total, cudaStream_t s);
+template <typename T>
+cudaError_t im_pdir_k(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, const KrylovDev *K, int64_t total,
+                      cudaStream_t s);
 template <typename T>
 cudaError_t im_mfield(vec2<T> *out, const vec2<T> *M, const vec2<T> *x, int64_t total, cudaStream_t s);
 

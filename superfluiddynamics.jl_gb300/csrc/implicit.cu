@@ -236,14 +236,76 @@ __global__ void k_im_axmy(vec2<T> *__restrict__ out, const vec2<T> *__restrict__
     }
 }
 
-// phi = (phi + alpha p) + omega s;  r = s - omega As
-template <typename T>
-__global__ void k_im_update(vec2<T> *__restrict__ phi, const vec2<T> *__restrict__ p, const vec2<T> *__restrict__ s,
-                            const vec2<T> *__restrict__ As, vec2<T> *__restrict__ r, double alpha, double omega,
-                            int64_t total)
+// ---- the solve's scalars on the device (one thread each; KrylovDev)
+
+// normb = sqrt(b.b) (or |M b|), a fresh solve
+__global__ void k_kry_init(KrylovDev *K, const double *__restrict__ dots)
 {
     pdl_enter();
-    const T a = (T)alpha, w = (T)omega;
+    K->normb = sqrt(dots[0]);
+    K->rr2 = K->alpha = K->omega = K->beta = 0.0;
+    K->done = K->niter = K->nonfinite = K->it = 0;
+}
+// iteration it: rr2 = r.r2, alpha = rr2 / (Ap.r2)
+__global__ void k_kry_alpha(KrylovDev *K, const double *__restrict__ dots)
+{
+    pdl_enter();
+    if (K->done) return;
+    K->it += 1;
+    K->rr2 = dots[0];
+    K->alpha = dots[0] / dots[1];
+}
+// omega = (As.s) / (As.As)
+__global__ void k_kry_omega(KrylovDev *K, const double *__restrict__ dots)
+{
+    pdl_enter();
+    if (K->done) return;
+    K->omega = dots[0] / dots[1];
+}
+// the stopping test on |r| / normb, then niter = it and beta = (r.r2) / rr2 *
+// alpha / omega; the last allowed iteration ends the solve
+__global__ void k_kry_check(KrylovDev *K, const double *__restrict__ dots, double tol, int nkrylov)
+{
+    pdl_enter();
+    if (K->done) return;
+    const double rr = dots[0];
+    if (!isfinite(rr)) {
+        K->nonfinite = 1;
+        K->done = 1;
+        return;
+    }
+    if (sqrt(rr) / K->normb < tol) {
+        K->done = 1;
+        return;
+    }
+    K->niter = K->it;
+    K->beta = dots[1] / K->rr2 * K->alpha / K->omega;
+    if (K->it >= nkrylov) K->done = 1;
+}
+
+// s = r - alpha Ap (alpha from the device)
+template <typename T>
+__global__ void k_im_axmy_k(vec2<T> *__restrict__ out, const vec2<T> *__restrict__ x, const vec2<T> *__restrict__ y,
+                            const KrylovDev *__restrict__ K, int64_t total)
+{
+    pdl_enter();
+    if (K->done) return;
+    const T a = (T)K->alpha;
+    GRID_LOOP(e, total) {
+        const vec2<T> u = x[e], w = y[e];
+        out[e] = mk<vec2<T>>(u.x - a * w.x, u.y - a * w.y);
+    }
+}
+
+// phi = (phi + alpha p) + omega s;  r = s - omega As
+template <typename T>
+__global__ void k_im_update_k(vec2<T> *__restrict__ phi, const vec2<T> *__restrict__ p,
+                              const vec2<T> *__restrict__ s, const vec2<T> *__restrict__ As, vec2<T> *__restrict__ r,
+                              const KrylovDev *__restrict__ K, int64_t total)
+{
+    pdl_enter();
+    if (K->done) return;
+    const T a = (T)K->alpha, w = (T)K->omega;
     GRID_LOOP(e, total) {
         const vec2<T> f = phi[e], pp = p[e], ss = s[e], aa = As[e];
         phi[e] = mk<vec2<T>>((f.x + a * pp.x) + w * ss.x, (f.y + a * pp.y) + w * ss.y);
@@ -253,11 +315,12 @@ __global__ void k_im_update(vec2<T> *__restrict__ phi, const vec2<T> *__restrict
 
 // p = r + beta (p - omega Ap)
 template <typename T>
-__global__ void k_im_pdir(vec2<T> *__restrict__ p, const vec2<T> *__restrict__ r, const vec2<T> *__restrict__ Ap,
-                          double beta, double omega, int64_t total)
+__global__ void k_im_pdir_k(vec2<T> *__restrict__ p, const vec2<T> *__restrict__ r, const vec2<T> *__restrict__ Ap,
+                            const KrylovDev *__restrict__ K, int64_t total)
 {
     pdl_enter();
-    const T bt = (T)beta, w = (T)omega;
+    if (K->done) return;
+    const T bt = (T)K->beta, w = (T)K->omega;
     GRID_LOOP(e, total) {
         const vec2<T> pp = p[e], rr = r[e], aa = Ap[e];
         const T qx = pp.x - w * aa.x, qy = pp.y - w * aa.y;
@@ -341,19 +404,48 @@ cudaError_t im_axmy(vec2<T> *out, const vec2<T> *x, double alpha, const vec2<T> 
     return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t im_update(vec2<T> *phi, const vec2<T> *p, const vec2<T> *sv, const vec2<T> *As, vec2<T> *r, double alpha,
-                      double omega, int64_t total, cudaStream_t s)
+cudaError_t kry_init(KrylovDev *K, const double *dots, cudaStream_t s)
 {
-    launch_pdl(k_im_update<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, p, sv, As, r, alpha, omega, total);
+    launch_pdl(k_kry_init, dim3(1), dim3(1), 0, s, K, dots);
+    return cudaGetLastError();
+}
+cudaError_t kry_alpha(KrylovDev *K, const double *dots, cudaStream_t s)
+{
+    launch_pdl(k_kry_alpha, dim3(1), dim3(1), 0, s, K, dots);
+    return cudaGetLastError();
+}
+cudaError_t kry_omega(KrylovDev *K, const double *dots, cudaStream_t s)
+{
+    launch_pdl(k_kry_omega, dim3(1), dim3(1), 0, s, K, dots);
+    return cudaGetLastError();
+}
+cudaError_t kry_check(KrylovDev *K, const double *dots, double tol, int nkrylov, cudaStream_t s)
+{
+    launch_pdl(k_kry_check, dim3(1), dim3(1), 0, s, K, dots, tol, nkrylov);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t im_pdir(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, double beta, double omega, int64_t total,
-                    cudaStream_t s)
+cudaError_t im_axmy_k(vec2<T> *out, const vec2<T> *x, const vec2<T> *y, const KrylovDev *K, int64_t total,
+                      cudaStream_t s)
 {
-    launch_pdl(k_im_pdir<T>, dim3(im_grid(total)), dim3(256), 0, s, p, r, Ap, beta, omega, total);
+    launch_pdl(k_im_axmy_k<T>, dim3(im_grid(total)), dim3(256), 0, s, out, x, y, K, total);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t im_update_k(vec2<T> *phi, const vec2<T> *p, const vec2<T> *sv, const vec2<T> *As, vec2<T> *r,
+                        const KrylovDev *K, int64_t total, cudaStream_t s)
+{
+    launch_pdl(k_im_update_k<T>, dim3(im_grid(total)), dim3(256), 0, s, phi, p, sv, As, r, K, total);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t im_pdir_k(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, const KrylovDev *K, int64_t total,
+                      cudaStream_t s)
+{
+    launch_pdl(k_im_pdir_k<T>, dim3(im_grid(total)), dim3(256), 0, s, p, r, Ap, K, total);
     return cudaGetLastError();
 }
 
@@ -369,10 +461,12 @@ cudaError_t im_pdir(vec2<T> *p, const vec2<T> *r, const vec2<T> *Ap, double beta
     template cudaError_t im_dot2<T>(const vec2<T> *, const vec2<T> *, const vec2<T> *, const vec2<T> *, int64_t,    \
                                     double *, double *, cudaStream_t);                                              \
     template cudaError_t im_axmy<T>(vec2<T> *, const vec2<T> *, double, const vec2<T> *, int64_t, cudaStream_t);    \
-    template cudaError_t im_update<T>(vec2<T> *, const vec2<T> *, const vec2<T> *, const vec2<T> *, vec2<T> *,      \
-                                      double, double, int64_t, cudaStream_t);                                       \
-    template cudaError_t im_pdir<T>(vec2<T> *, const vec2<T> *, const vec2<T> *, double, double, int64_t,           \
-                                    cudaStream_t);                                                                  \
+    template cudaError_t im_axmy_k<T>(vec2<T> *, const vec2<T> *, const vec2<T> *, const KrylovDev *, int64_t,      \
+                                      cudaStream_t);                                                                \
+    template cudaError_t im_update_k<T>(vec2<T> *, const vec2<T> *, const vec2<T> *, const vec2<T> *, vec2<T> *,    \
+                                        const KrylovDev *, int64_t, cudaStream_t);                                  \
+    template cudaError_t im_pdir_k<T>(vec2<T> *, const vec2<T> *, const vec2<T> *, const KrylovDev *, int64_t,      \
+                                      cudaStream_t);                                                                \
     template cudaError_t im_mfield<T>(vec2<T> *, const vec2<T> *, const vec2<T> *, int64_t, cudaStream_t);
 GPSS_IM_INST(float)
 GPSS_IM_INST(double)

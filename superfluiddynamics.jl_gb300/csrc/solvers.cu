@@ -152,13 +152,14 @@ template <typename T> static int rk_step_impl(gpss_ctx *c, int nsteps, int stepp
 struct ImBufs {
     void *r, *r2, *p, *Ap, *s, *As, *lap, *b, *M, *Anl2, *psim, *phi1, *phiw, *Anl;
     double *partials, *dots;
+    KrylovDev *kry;
 };
 
 template <typename T> static int im_bufs(gpss_ctx *c, ImBufs &B)
 {
     const size_t fb = (size_t)c->total * sizeof(vec2<T>);
     const size_t rb = (size_t)c->total * sizeof(T);
-    const size_t pb = sizeof(double) * (2 * 152 * 8 + 2);
+    const size_t pb = sizeof(double) * (2 * 152 * 8 + 2) + sizeof(KrylovDev);
     const size_t need = 13 * fb + rb + pb;
     if (!c->im_buf || c->im_bytes < need) {
         if (c->im_buf) { cudaStreamSynchronize(c->stream); cudaFree(c->im_buf); c->im_buf = nullptr; }
@@ -171,6 +172,7 @@ template <typename T> static int im_bufs(gpss_ctx *c, ImBufs &B)
     B.Anl = base + 13 * fb;
     B.partials = reinterpret_cast<double *>(base + 13 * fb + rb);
     B.dots = B.partials + 2 * 152 * 8;
+    B.kry = reinterpret_cast<KrylovDev *>(B.dots + 2);
     return GPSS_OK;
 }
 
@@ -205,43 +207,57 @@ static int im_apply(gpss_ctx *c, ImBufs &B, int scheme, double dt, const void *x
     return GPSS_OK;
 }
 
-// krylov! (precond = 0) / krylovPreCond! (precond = 1), krylov.jl:1-67
+// krylov! (precond = 0) / krylovPreCond! (precond = 1), krylov.jl:1-67.
+// The scalars and the stopping test live on the device (KrylovDev), so the
+// host issues iterations in chunks (2, 2, 4, 4, 8, ... up to 16) and reads the
+// solve's state back once per chunk; iterations issued past the end of the
+// solve leave phi, r and p untouched, so the result and the iteration count
+// are those of the reference's loop.
 template <typename T>
 static int im_krylov(gpss_ctx *c, ImBufs &B, int scheme, double dt, void *phi, int nkrylov, double tol, int precond,
                      int *niter_out)
 {
     using V = vec2<T>;
     const size_t fb = (size_t)c->total * sizeof(V);
-    double d[2];
+    const int64_t n = c->total;
     if (precond) {
-        IM_TRY(im_mfield<T>((V *)B.s, (const V *)B.M, (const V *)B.b, c->total, c->stream));
-        GPSS_TRY(im_dots<T>(c, B, B.s, B.s, nullptr, nullptr, d));
+        IM_TRY(im_mfield<T>((V *)B.s, (const V *)B.M, (const V *)B.b, n, c->stream));
+        IM_TRY(im_dot2<T>((const V *)B.s, (const V *)B.s, nullptr, nullptr, n, B.partials, B.dots, c->stream));
     } else {
-        GPSS_TRY(im_dots<T>(c, B, B.b, B.b, nullptr, nullptr, d));
+        IM_TRY(im_dot2<T>((const V *)B.b, (const V *)B.b, nullptr, nullptr, n, B.partials, B.dots, c->stream));
     }
-    const double normb = std::sqrt(d[0]);
+    IM_TRY(kry_init(B.kry, B.dots, c->stream));
     GPSS_TRY(im_apply<T>(c, B, scheme, dt, phi, true, precond, B.r));
     CUDA_TRY(c, cudaMemcpyAsync(B.r2, B.r, fb, cudaMemcpyDeviceToDevice, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(B.p, B.r, fb, cudaMemcpyDeviceToDevice, c->stream));
-    int niter = 0;
-    for (int it = 1; it <= nkrylov; it++) {
-        GPSS_TRY(im_apply<T>(c, B, scheme, dt, B.p, false, precond, B.Ap));
-        GPSS_TRY(im_dots<T>(c, B, B.r, B.r2, B.Ap, B.r2, d));
-        const double rr2 = d[0], alpha = d[0] / d[1];
-        IM_TRY(im_axmy<T>((V *)B.s, (const V *)B.r, alpha, (const V *)B.Ap, c->total, c->stream));
-        GPSS_TRY(im_apply<T>(c, B, scheme, dt, B.s, false, precond, B.As));
-        GPSS_TRY(im_dots<T>(c, B, B.As, B.s, B.As, B.As, d));
-        const double omega = d[0] / d[1];
-        IM_TRY(im_update<T>((V *)phi, (const V *)B.p, (const V *)B.s, (const V *)B.As, (V *)B.r, alpha, omega,
-                            c->total, c->stream));
-        GPSS_TRY(im_dots<T>(c, B, B.r, B.r, B.r, B.r2, d));
-        if (!std::isfinite(d[0])) return fail(c, GPSS_ENONFINITE, "Krylov solver: non-finite residual");
-        if (std::sqrt(d[0]) / normb < tol) break;
-        niter = it;
-        const double beta = d[1] / rr2 * alpha / omega;
-        IM_TRY(im_pdir<T>((V *)B.p, (const V *)B.r, (const V *)B.Ap, beta, omega, c->total, c->stream));
+    KrylovDev h{};
+    int issued = 0;
+    for (int chunk = 0; issued < nkrylov; chunk++) {
+        const int m = std::min(chunk < 6 ? 2 << (chunk / 2) : 16, nkrylov - issued);
+        for (int j = 0; j < m; j++) {
+            GPSS_TRY(im_apply<T>(c, B, scheme, dt, B.p, false, precond, B.Ap));
+            IM_TRY(im_dot2<T>((const V *)B.r, (const V *)B.r2, (const V *)B.Ap, (const V *)B.r2, n, B.partials,
+                              B.dots, c->stream));
+            IM_TRY(kry_alpha(B.kry, B.dots, c->stream));
+            IM_TRY(im_axmy_k<T>((V *)B.s, (const V *)B.r, (const V *)B.Ap, B.kry, n, c->stream));
+            GPSS_TRY(im_apply<T>(c, B, scheme, dt, B.s, false, precond, B.As));
+            IM_TRY(im_dot2<T>((const V *)B.As, (const V *)B.s, (const V *)B.As, (const V *)B.As, n, B.partials,
+                              B.dots, c->stream));
+            IM_TRY(kry_omega(B.kry, B.dots, c->stream));
+            IM_TRY(im_update_k<T>((V *)phi, (const V *)B.p, (const V *)B.s, (const V *)B.As, (V *)B.r, B.kry, n,
+                                  c->stream));
+            IM_TRY(im_dot2<T>((const V *)B.r, (const V *)B.r, (const V *)B.r, (const V *)B.r2, n, B.partials,
+                              B.dots, c->stream));
+            IM_TRY(kry_check(B.kry, B.dots, tol, nkrylov, c->stream));
+            IM_TRY(im_pdir_k<T>((V *)B.p, (const V *)B.r, (const V *)B.Ap, B.kry, n, c->stream));
+        }
+        issued += m;
+        CUDA_TRY(c, cudaMemcpyAsync(&h, B.kry, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if (h.done) break;
     }
-    *niter_out = niter;
+    if (h.nonfinite) return fail(c, GPSS_ENONFINITE, "Krylov solver: non-finite residual");
+    *niter_out = h.niter;
     return GPSS_OK;
 }
 
