@@ -73,6 +73,23 @@ def test_implicit_fp32(sfd, O, scheme):
     assert O.rel_l2(got, want) < 1e-5
 
 
+@pytest.mark.parametrize("scheme", ["BackwardEuler", "CrankNicolson"])
+@pytest.mark.parametrize("nkrylov", [1, 3, 5])
+def test_implicit_iteration_cap(sfd, O, scheme, nkrylov):
+    """Krylov solves capped below the iterations they need (krylov.jl's loop
+    runs at most nkrylov iterations and counts them): the device-side loop,
+    which issues iterations in chunks and stops at the cap, ends every solve
+    where the reference's loop does, with the same count and field."""
+    shape, b = (32, 32), ((-5.0, 5.0), (-4.0, 4.0))
+    psi = _gauss(shape, b)
+    V = O.quadratic_potential(shape, b)
+    kw = dict(coeffD=-0.5, beta=5.0, omega=0.2, dt=1e-2, nkrylov=nkrylov, tolkrylov=1e-12)
+    got, ng = run_implicit(sfd, scheme, shape, b, psi, V, nsteps=2, **kw)
+    want, nw = O.c_implicit_step(psi, b, scheme=scheme, V=V, nsteps=2, **kw)
+    assert ng == nw
+    assert O.rel_l2(got, want) < 1e-10
+
+
 def _solver_fixture(name):
     import os
     z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".solver.npz"))
