@@ -339,7 +339,9 @@ int64_t gpss_device_bytes(const gpss_ctx *ctx);
  * that loads it until the process exits.  Fields whose largest reduction
  * needs more partial sums than fit are rejected with GPSS_EINVAL (256^3 fits).
  * The first call on a device looks that array up; make it before any stream
- * capture.  The address is kept for the life of the process: a
+ * capture.  Every call copies its small coordinate and twiddle tables from
+ * host memory into the array and waits for `stream` before it returns.  The
+ * address is kept for the life of the process: a
  * cudaDeviceReset between calls is not supported.  Calls share the array:
  * calls that overlap on the GPU race, so serialise them.  Returns 0 or a
  * negative GPSS_E* code; the message is available from gpss_last_error(NULL).
