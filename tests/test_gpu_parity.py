@@ -613,13 +613,15 @@ def test_fullsize_time_reversal_fp32(sfd, O, W, compensated, bar):
 
 # ----------------------------------------------------------- energy cache --
 @pytest.mark.parametrize("omega", [0.0, 0.4])
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp32c"])
 def test_energy_cache_solve(sfd, O, precision, omega):
     """GPSS_FLAG_ENERGY_CACHE: solve!'s energy-then-timeStep! sequence gives
     the same energy records as without the cache, with fewer passes per
     iteration (none beyond the step at Omega = 0, one read-only x pass with
     rotation, against 3); the cache follows every change of the field and of
-    the parameters."""
+    the parameters.  fp32c: FP32 with the compensated passes."""
+    comp = precision == "fp32c"
+    precision = "fp32" if comp else precision
     shape, bounds = (32, 16, 8), ((-5.0, 5.0), (-4.0, 4.0), (-3.0, 3.0))
     psi0 = random_field(shape, seed=5)
     V = O.quadratic_potential(shape, bounds)
@@ -630,7 +632,7 @@ def test_energy_cache_solve(sfd, O, precision, omega):
         f = sfd.Field(g)
         f.phi = psi0
         p = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=-0.5, beta=30.0, Omega=omega)
-        n = sfd.NumModelSplit2(f, p, 2e-3, 20, 100, precision=precision, energy_cache=cache)
+        n = sfd.NumModelSplit2(f, p, 2e-3, 20, 100, precision=precision, energy_cache=cache, compensated=comp)
         l0 = L.gpss_launch_count(n.handle)
         res[cache] = np.array(sfd.solve(n))
         launches[cache] = L.gpss_launch_count(n.handle) - l0
@@ -640,7 +642,7 @@ def test_energy_cache_solve(sfd, O, precision, omega):
             n.upload()
             f2 = sfd.Field(sfd.Grid(shape, bounds))
             f2.phi = psi0
-            fresh = sfd.NumModelSplit2(f2, p, 2e-3, 1, 1, precision=precision)
+            fresh = sfd.NumModelSplit2(f2, p, 2e-3, 1, 1, precision=precision, compensated=comp)
             assert np.allclose(n.energies(), fresh.energies(), rtol=1e-12, atol=0)
             p2 = sfd.GrossPitaevskiiParameters(sfd.PotentialArray(f, V), coeffD=-0.5, beta=10.0, Omega=omega)
             n.step(3)
