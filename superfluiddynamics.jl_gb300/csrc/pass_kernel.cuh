@@ -96,10 +96,9 @@ enum { NL_NONE = 0, NL_REAL = 1, NL_IMAG = 2 };
 //   FEAT_GRIDM (with FEAT_COMP, without FEAT_DIAG) one grid for the whole
 //              pass from the mass bound `grid_mass` instead of a grid per
 //              thread and stage (no re-gridding between stages)
-//   FEAT_TMA   (FP32 y/z columns of a 3D field, with FEAT_NONE or FEAT_NL,
-//              or with FEAT_COMP | FEAT_GRIDM) each tile arrives in shared
-//              memory by one tensor copy (TMA, `tmap`), issued while the
-//              previous tile is transformed
+//   FEAT_TMA   (FP32 y/z columns of a 3D field, with FEAT_NONE or FEAT_NL)
+//              each tile arrives in shared memory by one tensor copy (TMA,
+//              `tmap`), issued while the previous tile is transformed
 enum { FEAT_NONE = 0, FEAT_NL = 1, FEAT_DIAG = 2, FEAT_ALL = 3, FEAT_PLANE = 4, FEAT_IMAGM = 8, FEAT_ADJ = 16,
        FEAT_SMALL = 32, FEAT_MASK = 64, FEAT_ACC = 128, FEAT_COMP = 256, FEAT_GRIDM = 512, FEAT_TMA = 1024 };
 
