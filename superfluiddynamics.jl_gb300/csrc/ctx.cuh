@@ -70,7 +70,6 @@ struct gpss_ctx {
     // FP32 3D fields: tensor maps of psi for the y and z passes' tile copies
     // (two CUtensorMap, 64-byte aligned, in device memory); null if unused
     void *tmap_dev = nullptr;
-    bool tmap_comp = false;  // tmap_dev also holds the compensated passes' maps (entries 2, 3)
     double *sums = nullptr;   // [4][RQ_COUNT]: slots 0..2 per axis, slot 3 diagnostics
     double *scale = nullptr;  // ScaleCell: the factor in FP64 and as a float
     int *status = nullptr;    // [1]
@@ -439,9 +438,9 @@ static int kinetic_fused(gpss_ctx *c, double dtl, int imag, bool nl, double dtnl
         // plain FP32 y/z passes of psi under the mass lock (the call checks
         // the status word, where a tile copy that timed out is reported):
         // tiles arrive by tensor copies
-        if (c->tmap_dev && (!a.comp || c->tmap_comp) && axis >= 1 && field == c->psi && fin_last == FIN_MASSLOCK &&
-            !diag_kin && a.prow == 0) {
-            a.tmap = (const char *)c->tmap_dev + ((a.comp ? 2 : 0) + axis - 1) * sizeof(CUtensorMap);
+        if (c->tmap_dev && !a.comp && axis >= 1 && field == c->psi && fin_last == FIN_MASSLOCK && !diag_kin &&
+            a.prow == 0) {
+            a.tmap = (const char *)c->tmap_dev + (axis - 1) * sizeof(CUtensorMap);
             a.taxis = axis;
             a.tnx = (int)c->n[0];
             a.fin_status = c->status;

@@ -182,36 +182,22 @@ static int make_tensor_maps(gpss_ctx *c)
         cudaGetLastError();
         return GPSS_OK;
     }
-    // maps[0..1]: y, z boxes of the plain passes' W columns; maps[2..3]: the
-    // compensated passes' (their CTAs are smaller)
-    CUtensorMap maps[4];
+    CUtensorMap maps[2];
     std::memset(maps, 0, sizeof(maps));
     const cuuint64_t dims[3] = {(cuuint64_t)c->n[0], (cuuint64_t)c->n[1], (cuuint64_t)c->n[2]};
     const cuuint64_t strides[2] = {(cuuint64_t)c->n[0] * 8, (cuuint64_t)(c->n[0] * c->n[1]) * 8};
     const cuuint32_t estr[3] = {1, 1, 1};
-    bool comp_ok = GPSS_COMP_TMA != 0;
-    for (int set = 0; set < 2; set++) {
-        for (int axis = 1; axis <= 2; axis++) {
-            const int64_t n = c->n[axis];
-            const int W = set == 0 ? PassLauncher<float>::lines((int)n, false) : comp_col_lines((int)n);
-            const bool fits = n >= 64 && W >= 2 && c->n[0] % W == 0;
-            if (set == 0 && !fits) return GPSS_OK;
-            if (set == 1 && (!fits || !comp_ok)) {
-                comp_ok = false;
-                continue;
-            }
-            const cuuint32_t box[3] = {(cuuint32_t)W, axis == 1 ? (cuuint32_t)n : 1u, axis == 2 ? (cuuint32_t)n : 1u};
-            const CUresult r = reinterpret_cast<EncodeFn>(fn)(
-                &maps[2 * set + axis - 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, c->psi, dims, strides, box, estr,
-                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            if (r != CUDA_SUCCESS) {
-                if (set == 0) return GPSS_OK;
-                comp_ok = false;
-            }
-        }
+    for (int axis = 1; axis <= 2; axis++) {
+        const int64_t n = c->n[axis];
+        const int W = PassLauncher<float>::lines((int)n, false);
+        if (n < 64 || W < 2 || c->n[0] % W) return GPSS_OK;
+        const cuuint32_t box[3] = {(cuuint32_t)W, axis == 1 ? (cuuint32_t)n : 1u, axis == 2 ? (cuuint32_t)n : 1u};
+        const CUresult r = reinterpret_cast<EncodeFn>(fn)(
+            &maps[axis - 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, c->psi, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return GPSS_OK;
     }
-    c->tmap_comp = comp_ok;
     GPSS_TRY(dev_alloc(c, &c->tmap_dev, sizeof(maps)));
     CUDA_TRY(c, cudaMemcpy(c->tmap_dev, maps, sizeof(maps), cudaMemcpyHostToDevice));
     return GPSS_OK;
@@ -808,13 +794,6 @@ int gpss_time_pass(gpss_ctx *c, int axis, int mode, int reps, double dt, double 
         if (a.comp) {  // the mass bound of the real-time passes (the mass-lock target slot)
             GPSS_TRY(diag_passes<T>(c, false, FIN_NONE));
             a.grid_mass = c->sums + kDiagSlot * RQ_COUNT + RQ_MASS;
-            if (c->tmap_comp && axis >= 1) {  // the tensor-copy tiles of the real-time y/z passes
-                a.tmap = (const char *)c->tmap_dev + (2 + axis - 1) * sizeof(CUtensorMap);
-                a.taxis = axis;
-                a.tnx = (int)c->n[0];
-                a.fin_status = c->status;
-                CUDA_TRY(c, cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
-            }
         } else if (c->tmap_dev && axis >= 1) {  // the tensor-copy tiles of the real-time y/z passes
             a.tmap = (const char *)c->tmap_dev + (axis - 1) * sizeof(CUtensorMap);
             a.taxis = axis;

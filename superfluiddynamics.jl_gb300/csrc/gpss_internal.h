@@ -84,12 +84,6 @@ cudaError_t launch_pass_f64(int mode, bool xl, int n, const PassArgs<double> &a,
                             cudaStream_t s);
 int pass_lines_per_cta_f32(int n, bool xl);
 int pass_lines_per_cta_f64(int n, bool xl);
-// columns per CTA of the compensated FP32 y/z passes (their tensor-map box width)
-inline int comp_col_lines(int n)
-{
-    const int n1 = n < 16 ? n : 16;
-    return GPSS_PASS_THREADS_COL_COMP_F32 / (n / n1);
-}
 // pipelined fused pass (n in {64, 128, 256}; tiles of 4096/n lines)
 cudaError_t launch_pipe_f32(bool xl, int n, const PassArgs<float> &a, int ntiles, cudaStream_t s);
 cudaError_t launch_pipe_f64(bool xl, int n, const PassArgs<double> &a, int ntiles, cudaStream_t s);

@@ -91,13 +91,6 @@ static cudaError_t launch_comp_mode(const PassArgs<float> &a, int blocks, cudaSt
     }
     if (diag) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_ALL>(a, blocks, s);
     if (a.grid_mass) {  // one grid per pass from the mass bound
-        if constexpr (!XL && N >= 64 && GPSS_COMP_TMA) {
-            if (a.tmap) {  // y/z columns of a 3D field: tiles arrive by tensor copy
-                constexpr int F = FEAT_COMP | FEAT_GRIDM | FEAT_TMA;
-                if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, F | FEAT_NL>(a, blocks, s);
-                return launch_pass_inst<float, N, XL, MODE_FUSED, F>(a, blocks, s);
-            }
-        }
         if (nl) return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_GRIDM | FEAT_NL>(a, blocks, s);
         return launch_pass_inst<float, N, XL, MODE_FUSED, FEAT_COMP | FEAT_GRIDM>(a, blocks, s);
     }

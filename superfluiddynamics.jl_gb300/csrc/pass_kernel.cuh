@@ -293,18 +293,9 @@ template <typename T, bool XL, int FEAT = 0> struct PassGeom {
 // waves instead of 2.25 (the 512-run batch 44.1 -> 43.5 ms per 500 steps)
 #define GPSS_PASS_SM_THREADS_PLANE_XL_F32 896
 #endif
-// Compensated y/z passes whose tiles arrive by tensor copy (FEAT_COMP |
-// FEAT_TMA): the 16 KB staging tile leaves room for 3 CTAs per SM.
-#ifndef GPSS_COMP_TMA
-#define GPSS_COMP_TMA 1
-#endif
-#ifndef GPSS_PASS_SM_THREADS_COMP_TMA_F32
-#define GPSS_PASS_SM_THREADS_COMP_TMA_F32 384
-#endif
 template <typename T, bool XL, int MODE, int FEAT> struct PassOcc {
     static constexpr int SM_THREADS =
-        ((FEAT & FEAT_COMP) && (FEAT & FEAT_TMA)) ? GPSS_PASS_SM_THREADS_COMP_TMA_F32
-        : (FEAT & FEAT_COMP) ? GPSS_PASS_SM_THREADS_COMP_F32
+        (FEAT & FEAT_COMP) ? GPSS_PASS_SM_THREADS_COMP_F32
         : (MODE == MODE_FUSED && (FEAT & ~FEAT_SMALL) == FEAT_NONE)
             ? (XL ? GPSS_PASS_SM_THREADS_LEAN_XL_F32 : GPSS_PASS_SM_THREADS_LEAN_F32)
         : (MODE == MODE_FUSED && FEAT == FEAT_IMAGM)
@@ -450,9 +441,8 @@ pass_kernel(const PassArgs<T> a)
     constexpr bool kComp = (FEAT & FEAT_COMP) != 0 && sizeof(T) == 4;
     static_assert(!kComp || (MODE == MODE_FUSED && !kMask && !kPlane && !kImagM), "compensated: fused kinetic passes");
     constexpr bool kTma = PassShape<T, N, XL, FEAT>::TMA;
-    static_assert(!kTma || (MODE == MODE_FUSED && !kDiag && !kPlane && !kImagM && !kMask && !kAdj &&
-                            (!kComp || (FEAT & FEAT_GRIDM))),
-                  "tensor-copy tiles: kinetic (+NL) passes, compensated ones on the mass-bound grid");
+    static_assert(!kTma || (MODE == MODE_FUSED && !kComp && !kDiag && !kPlane && !kImagM && !kMask && !kAdj),
+                  "tensor-copy tiles: plain kinetic (+NL) passes");
     const int red = a.red & ((kDiag ? (RED_POINT | RED_KIN) : 0) | (kNL || kDiag || kImagM ? RED_MASS : 0));
     const int64_t prow = kDiag ? a.prow : 0;
     using V = vec2<T>;
@@ -678,21 +668,7 @@ pass_kernel(const PassArgs<T> a)
             }
         }
         if constexpr (N2 > 1) {
-            if constexpr (kTma) {
-                // every thread has read the staging tile: the next tile's copy
-                // may land in it (a copy that timed out stops the CTA here,
-                // as in the plain passes)
-                if (__syncthreads_or(tdead)) {
-                    if (tid == 0) {
-                        mbar_wait_bounded(tbar, tphase ^ 1u, kTmaWaitPolls);
-                        if (a.fin_status) atomicOr(a.fin_status, 2);
-                    }
-                    break;
-                }
-                if (tid == 0 && tile + (int)gridDim.x < ntiles) tma_issue(tile + (int)gridDim.x);
-            } else {
-                line_sync();
-            }
+            line_sync();
             constexpr int NI = N1 / N2;
 #pragma unroll
             for (int i = 0; i < NI; i++) {
